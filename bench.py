@@ -1,0 +1,424 @@
+"""Benchmark: PSkel iterative stencils on one GB300.
+
+Default workload (the headline configuration): Game of Life, Moore mask,
+uint8 cells Bernoulli(0.3) from a seed, 8192 x 8192 grid, 1000 generations
+per step, temporal blocking of 16 generations per pass. A "step" is one full
+1000-generation run over the grid.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload life|jacobi|advect|advect_bf16|jacobi_bf16]
+
+Prints ONE JSON line. ``value`` is GCells/s (cell updates per second) with the
+grid resident in HBM; ``e2e`` is the same metric through the host entry point
+(pskel_run2d_host: host->device copy from pinned memory, the run, the copy
+back). ``--impl reference`` times the reference's own OpenMP runIterativeCPU
+(oracle/_ref/pskel_ref, built from the reference headers) on the host cores on
+a bounded sample of the same workload.
+
+Under torchrun (N > 1) every rank runs an independent replica of the
+workload on its own GPU (the path has no cross-grid exchange); the timing is
+the max over ranks and ``value`` counts the cells of all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GCells/s"
+WORKLOADS = {
+    "life": dict(desc="Game of Life 2D Moore 8-neighbour mask, uint8 Bernoulli(0.3), 8192x8192, 1000 iterations",
+                 W=8192, H=8192, iters=1000, dtype="u8", T=16, b_alg=2),
+    "jacobi": dict(desc="Jacobi 2D 5-point (4 neighbours, weight 0.25), float32 1024x1024, zero ring, 100 iterations",
+                   W=1024, H=1024, iters=100, dtype="f32", T=8, b_alg=8),
+    "jacobi_bf16": dict(desc="Jacobi 2D 5-point, bf16 storage / fp32 arithmetic, 1024x1024, 100 iterations",
+                        W=1024, H=1024, iters=100, dtype="bf16", T=8, b_alg=4),
+    "advect": dict(desc="advection-diffusion 2D, float32 4096x4096, winds N(0,0.1), K 0.1, dt 0.2, 500 iterations",
+                   W=4096, H=4096, iters=500, dtype="f32", T=4, b_alg=16),
+    "advect_bf16": dict(desc="advection-diffusion 2D, bf16 storage / fp32 arithmetic, 4096x4096, 500 iterations",
+                        W=4096, H=4096, iters=500, dtype="bf16", T=4, b_alg=8),
+}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- our arm
+
+def make_inputs(wl):
+    from pskel_gb300 import synth as S
+    name = wl["name"]
+    W, H = wl["W"], wl["H"]
+    if name == "life":
+        a, b = S.life(W, H, seed=1)
+        return {"in": a, "out": b}
+    if name.startswith("jacobi"):
+        a, b = S.jacobi2d(W, H, seed=1)
+        if wl["dtype"] == "bf16":
+            a, b = S.f32_to_bf16(a), S.f32_to_bf16(b)
+        return {"in": a, "out": b}
+    if name.startswith("advect"):
+        a, b, u, v = S.advect2d(W, H, seed=1)
+        if wl["dtype"] == "bf16":
+            a, b, u, v = (S.f32_to_bf16(x) for x in (a, b, u, v))
+        return {"in": a, "out": b, "u": u, "v": v}
+    raise ValueError(name)
+
+
+def stencil_for(wl, P, S, keep, wind=(None, None)):
+    name = wl["name"]
+    if name == "life":
+        return P.make_stencil(P.OP_LIFE, "u8", S.MOORE8_OFFSETS, keep=keep)
+    if name.startswith("jacobi"):
+        return P.make_stencil(P.OP_LINEAR, wl["dtype"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    return P.make_stencil(P.OP_ADVECT, wl["dtype"], S.JACOBI4_OFFSETS, wind=wind, K=S.ADVECT_K, dt=S.ADVECT_DT,
+                          inv_dx=S.ADVECT_INV_DX, keep=keep)
+
+
+def run_ours(args, wl, world, rank, local):
+    import torch
+
+    import pskel_gb300 as P
+    from pskel_gb300 import synth as S
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    x = make_inputs(wl)
+    W, H, iters = wl["W"], wl["H"], wl["iters"]
+    tview = (lambda a: torch.from_numpy(a.view(np.int16))) if wl["dtype"] == "bf16" else torch.from_numpy
+    src0 = tview(x["in"]).to(dev)
+    out0 = tview(x["out"]).to(dev)
+    a = src0.clone()
+    b = out0.clone()
+    keep = P._Keep()
+    wind_dev = (None, None)
+    if "u" in x:
+        ud, vd = tview(x["u"]).to(dev), tview(x["v"]).to(dev)
+        wind_dev = (ud.data_ptr(), vd.data_ptr())
+    st = stencil_for(wl, P, S, keep, wind_dev)
+    sch = P.Schedule(time_steps=args.time_steps or wl["T"], tile_w=0, tile_h=args.tile_h, tile_d=0, ctas=0)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)  # 512 MB > L2
+
+    def one_step():
+        P.iterate2d(st, a, b, iters, sched=sch, stream=stream.cuda_stream)
+
+    def reset():
+        with torch.cuda.stream(stream):
+            a.copy_(src0)
+            b.copy_(out0)
+            flush.fill_(1)
+
+    for _ in range(args.warmup):
+        reset()
+        one_step()
+    P.sync(stream.cuda_stream)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            reset()
+            starts[k].record(stream)
+            one_step()
+            ends[k].record(stream)
+        P.sync(stream.cuda_stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    dist_barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_dev = dist_max(sum(step_ms) / 1e3, world)
+    cells = W * H * iters
+    value = world * cells * args.steps / t_dev / 1e9
+
+    # result check against a schedule-independent property: the same run with
+    # one generation per pass gives identical cells (the first step's result).
+    passes = P.lib.pskel_plan_passes(iters, sch.time_steps, None, 0)
+    launches = passes * args.steps
+
+    # kernel-only launch timing for the roofline: average pass duration
+    per_launch_ms = sum(step_ms) / args.steps / passes
+
+    # ---- end to end through the host entry point, pinned host buffers
+    pin_in = torch.from_numpy(x["in"].view(np.int16) if wl["dtype"] == "bf16" else x["in"]).pin_memory()
+    pin_out0 = torch.from_numpy(x["out"].view(np.int16) if wl["dtype"] == "bf16" else x["out"]).pin_memory()
+    pin_out = pin_out0.clone().pin_memory()
+    wind_host = (None, None)
+    if "u" in x:
+        pu = torch.from_numpy(x["u"].view(np.int16) if wl["dtype"] == "bf16" else x["u"]).pin_memory()
+        pv = torch.from_numpy(x["v"].view(np.int16) if wl["dtype"] == "bf16" else x["v"]).pin_memory()
+        wind_host = (pu.data_ptr(), pv.data_ptr())
+    st_h = stencil_for(wl, P, S, keep, wind_host)
+    esz = pin_in.element_size()
+    h2d = W * H * esz * (3 if "u" in x else 1)
+    r = 1
+    if iters % 2 == 1:
+        h2d += (2 * r * W + 2 * r * (H - 2 * r)) * esz
+    d2h = W * H * esz
+
+    def e2e_step():
+        pin_out.copy_(pin_out0)
+        P.lib.pskel_run2d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, iters, P.C.byref(sch))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    times = []
+    for _ in range(args.steps):
+        pin_out.copy_(pin_out0)
+        t1 = time.perf_counter()
+        rc = P.lib.pskel_run2d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, iters,
+                                    P.C.byref(sch))
+        times.append(time.perf_counter() - t1)
+        if rc != 0:
+            raise RuntimeError(P.lib.pskel_last_error().decode())
+    t_e2e = dist_max(sum(times), world)
+    e2e_value = world * cells * args.steps / t_e2e / 1e9
+    # the e2e result equals the device-resident run's result
+    res_dev = (b if iters % 2 == 1 else a).cpu()
+    # (the device run was reset between steps, so its final state is one run)
+    same = bool(torch.equal(res_dev, pin_out))
+
+    peak, peak_kind = load_peaks()
+    b_alg = wl["b_alg"]
+    achieved = b_alg * W * H * (iters / passes) / (per_launch_ms / 1e3) / 1e9
+    pass_bytes = b_alg * W * H  # the pass's own compulsory traffic: read + write the grid once
+    traffic = load_traffic(wl["name"])
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_dev / args.steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",
+        "config": {"workload": wl["desc"], "grid": [H, W], "iterations_per_step": iters,
+                   "time_steps_per_pass": sch.time_steps, "l2": "flushed between timed steps (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "GCells/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "matches_device_run": same},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 3), "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s",
+                     "per_launch_ms": round(per_launch_ms, 5),
+                     "pass_compulsory_frac": round(pass_bytes / (per_launch_ms / 1e3) / 1e9 / peak, 3),
+                     "note": "achieved = B_alg per cell update x cell updates per launch / launch time; "
+                             "temporal blocking fuses time_steps updates per HBM round trip, so frac can exceed 1; "
+                             "pass_compulsory_frac = one read + one write of the grid per launch / time / peak"},
+        "wall_s": round(wall, 3),
+    }
+    return line, clk.summary()
+
+
+def load_traffic(name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if name in d:
+            return d[name]
+    return None
+
+
+# ------------------------------------------------------- CPU baselines
+
+def cpu_sample(wl, threads, iters_sample, use_ref=True):
+    """Time the reference's runIterativeCPU (or the oracle port) on a sample."""
+    import oracle
+    x = make_inputs(wl)
+    W, H = wl["W"], wl["H"]
+    if use_ref and oracle.have_ref():
+        from pskel_gb300 import synth as S
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="close", OMP_PLACES="cores")
+        with tempfile.TemporaryDirectory() as d:
+            d = Path(d)
+            npt = x["in"].dtype
+            for k, v in x.items():
+                np.ascontiguousarray(v).tofile(d / k)
+            if wl["name"] == "life":
+                cmd = ["life", W, H, iters_sample, threads, d / "in", d / "out", d / "res"]
+            elif wl["name"].startswith("jacobi"):
+                with open(d / "m.txt", "w") as f:
+                    f.write("4 2\n" + "".join(f"{o[0]} {o[1]} {w!r}\n" for o, w in zip(S.JACOBI4_OFFSETS,
+                                                                                     S.JACOBI4_WEIGHTS)))
+                cmd = ["lin2d", wl["dtype"], W, H, iters_sample, threads, d / "m.txt", d / "in", d / "out", d / "res"]
+            else:
+                cmd = ["advect", wl["dtype"], W, H, iters_sample, threads, repr(S.ADVECT_K), repr(S.ADVECT_DT),
+                       repr(S.ADVECT_INV_DX), d / "in", d / "out", d / "u", d / "v", d / "res"]
+            out = subprocess.run([str(oracle.REF_BIN)] + [str(c) for c in cmd], capture_output=True, text=True,
+                                 env=env, check=True).stdout
+            wall = json.loads([l for l in out.splitlines() if l.startswith("{")][-1])["wall_s"]
+            del npt
+        return W * H * iters_sample / wall / 1e9, "reference", wall
+    oracle.build()
+    t0 = time.perf_counter()
+    if wl["name"] == "life":
+        oracle.life(x["in"], x["out"], iters_sample)
+    elif wl["name"].startswith("jacobi"):
+        from pskel_gb300 import synth as S
+        oracle.lin2d(x["in"], x["out"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters_sample, dtype=wl["dtype"])
+    else:
+        from pskel_gb300 import synth as S
+        oracle.advect(x["in"], x["out"], x["u"], x["v"], iters_sample, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX,
+                      dtype=wl["dtype"])
+    wall = time.perf_counter() - t0
+    return W * H * iters_sample / wall / 1e9, "port", wall
+
+
+def sample_iters(wl):
+    # about 1e9 cell updates: a few seconds on the host cores
+    return max(1, int(1e9 // (wl["W"] * wl["H"])))
+
+
+def run_reference_arm(args, wl, world, rank):
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    its = sample_iters(wl)
+    vals, kind, walls = [], None, []
+    for _ in range(args.warmup):
+        cpu_sample(wl, threads, max(1, its // 4))
+    for _ in range(args.steps):
+        v, kind, w = cpu_sample(wl, threads, its)
+        vals.append(v)
+        walls.append(w)
+    cells = wl["W"] * wl["H"] * its * args.steps
+    value = cells / sum(walls) / 1e9
+    sample = f"{wl['H']}x{wl['W']} grid, {its} iterations per step (of {wl['iters']}), {threads} OpenMP threads"
+    return {"metric": METRIC, "value": round(value, 4), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(sum(walls) / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": wl["desc"], "grid": [wl["H"], wl["W"]], "iterations_per_step": its},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": "GCells/s", "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "GCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="life", choices=sorted(WORKLOADS))
+    ap.add_argument("--time-steps", type=int, default=0)
+    ap.add_argument("--tile-h", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = dict(WORKLOADS[args.workload], name=args.workload)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        line = run_reference_arm(args, wl, world, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    line, clocks = run_ours(args, wl, world, rank, local)
+    line["clocks"] = clocks
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            its = sample_iters(wl)
+            v, kind, wall = cpu_sample(wl, os.cpu_count() or 1, its)
+            line["cpu_baseline"] = {"value": round(v, 4), "unit": "GCells/s", "cores": os.cpu_count() or 1,
+                                    "kind": kind, "sample": f"{wl['H']}x{wl['W']} grid, {its} iterations, "
+                                                            f"{wall:.2f} s"}
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+/*
+ * pskel_gb300 -- C ABI of the GB300 (sm_103a) iterative-stencil library.
+ *
+ * This is the drop-in boundary under PSkel's C++ skeleton API. The header
+ * templates in include/PSkel*.h (and any FFI binding) call these functions;
+ * they take plain pointers, sizes and descriptors, never C++ or torch types.
+ *
+ * Array layouts are the reference's (PSkelArray.hpp:349-352, 658-677): 2D
+ * element (h, w) at [h * pitch + w]; 3D element (h, w, d) at
+ * [(h * width + w) * depth + d] (d fastest).
+ *
+ * Semantics of one iterative run follow StencilBase::runIterativeGPU /
+ * runIterativeCPU (PSkelStencil.hpp:880-938, 1046-1097):
+ *   - iteration k reads one buffer and writes the other (ping-pong);
+ *   - 2D: only cells with r <= h < H-r and r <= w < W-r are written
+ *     (r = mask range), so each buffer keeps its own ring;
+ *   - 3D: every cell is written, neighbours outside the grid read
+ *     mask.halo_value (Mask3D::get, PSkelMask.hpp:186-199);
+ *   - after `iterations` steps the result is in `out` when iterations is odd
+ *     and in `in` when it is even (the device state runIterativeGPU copies
+ *     back from, :1083-1090). The *_host entry points do that copy back.
+ *
+ * Device entry points are asynchronous on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream). Kernel-side errors (a bounded wait that ran
+ * out, a Life cell outside {0,1}) are latched in a per-device error word;
+ * pskel_sync() waits for the stream and reports and clears it. Host entry
+ * points are synchronous and check it themselves.
+ *
+ * Not thread-safe, like the reference (its GA tuner uses a global evaluator,
+ * PSkelStencil.hpp:1866-1881): one caller thread per process.
+ */
+#ifndef PSKEL_GB300_H
+#define PSKEL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PSKEL_API __attribute__((visibility("default")))
+#else
+#define PSKEL_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t pskel_status;
+#define PSKEL_OK 0
+#define PSKEL_ERR_INVALID 1     /* bad argument: null pointer, size, mask shape */
+#define PSKEL_ERR_UNSUPPORTED 2 /* valid request outside the implemented kernels */
+#define PSKEL_ERR_CUDA 3        /* a CUDA runtime call failed (pskel_last_error) */
+#define PSKEL_ERR_DEVICE 4      /* a kernel latched an error (pskel_last_error) */
+#define PSKEL_ERR_NOMEM 5       /* device or pinned host allocation failed */
+
+typedef enum pskel_dtype {
+  PSKEL_U8 = 0,   /* uint8 cells (Game of Life) */
+  PSKEL_F32 = 1,  /* fp32 storage, fp32 arithmetic */
+  PSKEL_BF16 = 2  /* bf16 storage (rounded to nearest even every step), fp32 arithmetic */
+} pskel_dtype;
+
+typedef enum pskel_op {
+  /* out = sum_n weights[n] * in(neighbour n), products and sums in mask
+   * order without contraction. */
+  PSKEL_OP_LINEAR = 0,
+  /* Game of Life over the mask neighbourhood: s = sum of neighbours,
+   * out = (s == 3 || (s == 2 && c == 1)); the mask must be the 8 Moore
+   * offsets (any order). */
+  PSKEL_OP_LIFE = 1,
+  /* Upwind advection-diffusion on the 4-neighbour cross with per-cell winds
+   * (the arithmetic of the reference's CLOUDSIM kernel, PSkelStencil.hpp:347-387). */
+  PSKEL_OP_ADVECT = 2
+} pskel_op;
+
+/* Mirror of MaskBase/Mask2D/Mask3D (PSkelMask.h:48-218). */
+typedef struct pskel_mask {
+  int32_t size;           /* number of entries */
+  int32_t dimension;      /* 2 or 3 */
+  const int32_t* offsets; /* size*dimension host ints: (dh, dw[, dd]) per entry */
+  const float* weights;   /* size host floats (ignored by LIFE and ADVECT) */
+  float halo_value;       /* value read outside a 3D grid (Mask3D haloValue) */
+  int32_t range;          /* 0: max |offset| (MaskBase::getRange) */
+} pskel_mask;
+
+typedef struct pskel_stencil {
+  pskel_op op;
+  pskel_dtype dtype;
+  pskel_mask mask;
+  /* ADVECT only: per-cell wind fields, same dtype and layout as the grid.
+   * Device pointers for the device entry points, host pointers for *_host. */
+  const void* wind_u;
+  const void* wind_v;
+  float diffusivity; /* ADVECT: K */
+  float dt;          /* ADVECT: time step */
+  float inv_dx;      /* ADVECT: 1/dx */
+} pskel_stencil;
+
+/* Execution schedule. Changes only speed, never results. Zero fields take the
+ * library's defaults. */
+typedef struct pskel_schedule {
+  int32_t tile_w;     /* core tile width (cells) */
+  int32_t tile_h;     /* core tile height (cells) */
+  int32_t tile_d;     /* 3D: core tile depth (cells) */
+  int32_t time_steps; /* steps fused per pass over the grid (temporal block) */
+  int32_t ctas;       /* persistent CTAs per launch */
+} pskel_schedule;
+
+/* Library version (major*10000 + minor*100 + patch). */
+PSKEL_API int32_t pskel_version(void);
+
+/* Message for the last failing call on this thread, "" if none. */
+PSKEL_API const char* pskel_last_error(void);
+
+/* Wait for `stream`, then report and clear the device error word. */
+PSKEL_API pskel_status pskel_sync(void* stream);
+
+/* Splits `iterations` steps into passes of at most `time_steps` steps, with a
+ * pass count of the same parity as `iterations` (so the ping-pong over passes
+ * ends in the buffer a step-by-step ping-pong ends in). Writes at most `cap`
+ * pass lengths to `passes` and returns the number of passes (host only). */
+PSKEL_API int32_t pskel_plan_passes(int64_t iterations, int32_t time_steps, int32_t* passes, int32_t cap);
+
+/* Iterative 2D stencil on device buffers.
+ * Replaces StencilBase::runIterativeGPU(iterations, bx, by) and
+ * runIterativeGPU(iterations, pyramidHeight, bx, by) (PSkelStencil.h:258-259,
+ * PSkelStencil.hpp:943-1097) and runIterativeTilingGPU's inner temporal
+ * blocking (PSkelStencil.h:292, PSkelStencil.hpp:1663-1862): schedule.time_steps
+ * plays pyramidHeight / innerIterations, schedule.tile_* the tiling sizes.
+ * `pitch` is the row pitch in elements (0 = width). Both buffers are written
+ * (ping-pong); see the header comment for where the result ends. */
+PSKEL_API pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height,
+                             int64_t pitch, int64_t iterations, const pskel_schedule* sched, void* stream);
+
+/* Iterative 2D stencil on host arrays: the whole of runIterativeGPU
+ * (PSkelStencil.hpp:1046-1097): copy in, iterate, copy the result into
+ * `out_host`. `in_host` is not modified; `out_host` must hold the output
+ * array's initial contents (its ring is part of the result when iterations
+ * is odd). Synchronous. */
+PSKEL_API pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void* out_host, int64_t width,
+                              int64_t height, int64_t iterations, const pskel_schedule* sched);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSKEL_GB300_H */

@@ -1,0 +1,123 @@
+"""Build recipe for ``oracle/_ref``: the reference's own ``runIterativeCPU``.
+
+Test infrastructure only. The product never imports, links or runs anything
+under ``oracle/``; tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg
+of ``bench.py`` use it as the checker.
+
+The reference (PSkel, header-only C++) does not compile for the CPU as shipped:
+``PSkelArray.hpp`` defines three groups of CUDA-only members outside any
+``#ifdef PSKEL_CUDA`` guard (lines 209-230 ``hostAllocPinned``, 278-284
+``cudaHostMemCopy``, 501-509 ``copyToDevicePinned``/``copyFromDevicePinned``),
+uses ``memcpy`` without ``<cstring>`` (line 412), unconditionally includes
+``<tbb/scalable_allocator.h>`` (``PSkel.h:80``) and ``<xmmintrin.h>``
+(``PSkelArray.hpp:42``, only for ``_mm_malloc``/``_mm_free``).
+
+This script therefore:
+  1. copies the reference headers into ``oracle/_ref/src`` (git-ignored output
+     directory; nothing of the reference is committed),
+  2. wraps exactly those three line ranges of the copy in ``#ifdef PSKEL_CUDA``
+     after checking the sha256 of the original file, so a different reference
+     revision is refused instead of being patched blindly,
+  3. writes two shim headers (``tbb/scalable_allocator.h`` over malloc/free and
+     ``xmmintrin.h`` over posix_memalign, which also makes the build portable
+     to aarch64 hosts),
+  4. compiles ``oracle/ref_runner.cpp`` against the copy with
+     ``g++ -O3 -ffp-contract=off -fopenmp -DPSKEL_OMP`` into
+     ``oracle/_ref/pskel_ref``.
+
+Step 1-3 need the reference tree (default ``/root/reference``, or the
+``PSKEL_REFERENCE`` environment variable). Step 4 only needs ``oracle/_ref/src``,
+so on a machine without the reference the previously prepared copy is compiled.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+SRC = OUT / "src"
+SHIM = OUT / "shim"
+BIN = OUT / "pskel_ref"
+
+# sha256 of the reference PSkelArray.hpp the line ranges below were read from.
+ARRAY_HPP_SHA256 = "eee8c8e0c3e492be63452c199138c7b73d5ac7af7b0a2e8527e2e8d8c6d06fe6"
+# 1-based inclusive line ranges of PSkelArray.hpp that only make sense with CUDA.
+CUDA_ONLY_RANGES = [(209, 230), (278, 284), (501, 509)]
+
+SHIM_TBB = """// Shim for the oracle build: PSkel.h includes this header unconditionally.
+#pragma once
+#include <cstdlib>
+inline void* scalable_malloc(size_t n) { return std::malloc(n); }
+inline void scalable_free(void* p) { std::free(p); }
+"""
+
+SHIM_XMM = """// Shim for the oracle build: PSkelArray.hpp needs only _mm_malloc/_mm_free.
+#pragma once
+#include <cstdlib>
+inline void* _mm_malloc(size_t n, size_t a) {
+  void* p = nullptr;
+  if (a < sizeof(void*)) a = sizeof(void*);
+  if (posix_memalign(&p, a, n ? n : a)) return nullptr;
+  return p;
+}
+inline void _mm_free(void* p) { std::free(p); }
+"""
+
+
+def reference_include() -> Path | None:
+    root = Path(os.environ.get("PSKEL_REFERENCE", "/root/reference"))
+    inc = root / "include"
+    return inc if (inc / "PSkelStencil.hpp").is_file() else None
+
+
+def prepare_overlay(inc: Path) -> None:
+    """Copy the reference headers and guard the CUDA-only line ranges."""
+    SRC.mkdir(parents=True, exist_ok=True)
+    for f in sorted(inc.iterdir()):
+        if f.suffix in (".h", ".hpp"):
+            shutil.copyfile(f, SRC / f.name)
+    arr = SRC / "PSkelArray.hpp"
+    raw = (inc / "PSkelArray.hpp").read_bytes()
+    digest = hashlib.sha256(raw).hexdigest()
+    if digest != ARRAY_HPP_SHA256:
+        raise RuntimeError(f"unexpected PSkelArray.hpp revision (sha256 {digest}); "
+                           "line ranges of the overlay were read from another revision")
+    lines = raw.decode("latin-1").split("\n")
+    for lo, hi in sorted(CUDA_ONLY_RANGES, reverse=True):
+        lines.insert(hi, "#endif /* oracle overlay */")
+        lines.insert(lo - 1, "#ifdef PSKEL_CUDA /* oracle overlay */")
+    arr.write_bytes("\n".join(lines).encode("latin-1"))
+    (SHIM / "tbb").mkdir(parents=True, exist_ok=True)
+    (SHIM / "tbb" / "scalable_allocator.h").write_text(SHIM_TBB)
+    (SHIM / "xmmintrin.h").write_text(SHIM_XMM)
+
+
+def compile_runner() -> Path:
+    cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fopenmp", "-DPSKEL_OMP",
+           "-include", "cstring", "-I", str(SHIM), "-I", str(SRC),
+           "-w", str(HERE / "ref_runner.cpp"), "-o", str(BIN)]
+    subprocess.run(cmd, check=True)
+    return BIN
+
+
+def build(require: bool = False) -> Path | None:
+    """Prepare (when the reference tree is present) and compile ``pskel_ref``."""
+    inc = reference_include()
+    if inc is not None:
+        prepare_overlay(inc)
+    if not (SRC / "PSkelStencil.hpp").is_file():
+        if require:
+            raise RuntimeError("reference headers unavailable: no overlay copy in oracle/_ref/src")
+        return None
+    return compile_runner()
+
+
+if __name__ == "__main__":
+    path = build(require=True)
+    print(path)
+    sys.exit(0)

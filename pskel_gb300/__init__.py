@@ -1,0 +1,144 @@
+"""pskel_gb300: GB300-native iterative stencils behind PSkel's API.
+
+This Python module is a thin ctypes binding of the C ABI in
+``include/pskel_gb300.h`` (the library ``pskel_gb300/libpskel_gb300.so``),
+used by the tests and the benchmark. C++ applications use the drop-in headers
+``include/PSkel*.h`` instead. There is no CPU fallback: every call runs the
+CUDA kernels of the library, and importing this module raises if the library
+has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libpskel_gb300.so"
+
+PSKEL_OK, PSKEL_ERR_INVALID, PSKEL_ERR_UNSUPPORTED, PSKEL_ERR_CUDA, PSKEL_ERR_DEVICE, PSKEL_ERR_NOMEM = range(6)
+U8, F32, BF16 = 0, 1, 2
+OP_LINEAR, OP_LIFE, OP_ADVECT = 0, 1, 2
+_DTYPES = {"u8": U8, "f32": F32, "bf16": BF16}
+_ESIZE = {U8: 1, F32: 4, BF16: 2}
+
+
+class PskelError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"pskel status {status}: {msg}")
+        self.status = status
+
+
+class Mask(C.Structure):
+    _fields_ = [("size", C.c_int32), ("dimension", C.c_int32), ("offsets", C.POINTER(C.c_int32)),
+                ("weights", C.POINTER(C.c_float)), ("halo_value", C.c_float), ("range", C.c_int32)]
+
+
+class Stencil(C.Structure):
+    _fields_ = [("op", C.c_int), ("dtype", C.c_int), ("mask", Mask), ("wind_u", C.c_void_p),
+                ("wind_v", C.c_void_p), ("diffusivity", C.c_float), ("dt", C.c_float), ("inv_dx", C.c_float)]
+
+
+class Schedule(C.Structure):
+    _fields_ = [("tile_w", C.c_int32), ("tile_h", C.c_int32), ("tile_d", C.c_int32), ("time_steps", C.c_int32),
+                ("ctas", C.c_int32)]
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(LIB_PATH))
+    lib.pskel_version.restype = C.c_int32
+    lib.pskel_last_error.restype = C.c_char_p
+    lib.pskel_sync.argtypes = [C.c_void_p]
+    lib.pskel_iterate2d.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                    C.c_int64, C.POINTER(Schedule), C.c_void_p]
+    lib.pskel_plan_passes.argtypes = [C.c_int64, C.c_int32, C.POINTER(C.c_int32), C.c_int32]
+    lib.pskel_plan_passes.restype = C.c_int32
+    lib.pskel_run2d_host.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                     C.POINTER(Schedule)]
+    return lib
+
+
+lib = _load()
+
+
+def _check(status: int):
+    if status != PSKEL_OK:
+        raise PskelError(status, lib.pskel_last_error().decode())
+
+
+class _Keep:
+    """Holds the ctypes arrays a descriptor points to for the call's duration."""
+
+    def __init__(self):
+        self.refs = []
+
+
+def make_mask(offsets, weights=None, halo=0.0, rng=0, keep: _Keep | None = None) -> Mask:
+    offsets = [tuple(o) for o in offsets]
+    dim = len(offsets[0]) if offsets else 2
+    off = (C.c_int32 * (len(offsets) * dim))(*[int(x) for o in offsets for x in o])
+    m = Mask(size=len(offsets), dimension=dim, offsets=C.cast(off, C.POINTER(C.c_int32)), halo_value=float(halo),
+             range=int(rng))
+    if keep is not None:
+        keep.refs.append(off)
+    if weights is not None:
+        wt = (C.c_float * len(weights))(*[float(w) for w in weights])
+        m.weights = C.cast(wt, C.POINTER(C.c_float))
+        if keep is not None:
+            keep.refs.append(wt)
+    return m
+
+
+def make_stencil(op: int, dtype: str, offsets=(), weights=None, halo=0.0, rng=0, wind=(None, None), K=0.0, dt=0.0,
+                 inv_dx=0.0, keep: _Keep | None = None) -> Stencil:
+    st = Stencil(op=op, dtype=_DTYPES[dtype])
+    if offsets:
+        st.mask = make_mask(offsets, weights, halo, rng, keep)
+    else:
+        st.mask = Mask(size=0, dimension=2)
+    st.wind_u, st.wind_v = wind
+    st.diffusivity, st.dt, st.inv_dx = K, dt, inv_dx
+    return st
+
+
+def make_schedule(sched) -> Schedule | None:
+    if sched is None:
+        return None
+    if isinstance(sched, Schedule):
+        return sched
+    return Schedule(**sched)
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def iterate2d(st: Stencil, a_in, a_out, iterations: int, sched=None, pitch: int = 0, stream=None, width=None,
+              height=None):
+    """Device-buffer run (torch CUDA tensors or raw pointers). Asynchronous."""
+    H = height if height is not None else a_in.shape[0]
+    W = width if width is not None else a_in.shape[1]
+    sc = make_schedule(sched)
+    _check(lib.pskel_iterate2d(C.byref(st), _ptr(a_in), _ptr(a_out), W, H, pitch, iterations,
+                               C.byref(sc) if sc is not None else None, stream))
+
+
+def sync(stream=None):
+    _check(lib.pskel_sync(stream))
+
+
+def run2d_host(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int, sched=None):
+    """runIterativeGPU on host arrays: returns the output array (a_out is updated in place)."""
+    assert a_in.flags.c_contiguous and a_out.flags.c_contiguous
+    H, W = a_in.shape
+    sc = make_schedule(sched)
+    _check(lib.pskel_run2d_host(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, iterations,
+                                C.byref(sc) if sc is not None else None))
+    return a_out

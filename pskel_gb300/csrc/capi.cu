@@ -1,0 +1,474 @@
+// C ABI entry points (include/pskel_gb300.h): argument checks, schedule
+// geometry, tensor maps, the pass loop and the host-array round trip.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pskel_gb300.h"
+#include "capi_internal.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pskel {
+
+// ----------------------------------------------------------- error reporting
+
+static thread_local std::string g_last_error;
+
+pskel_status fail(pskel_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+pskel_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? PSKEL_ERR_NOMEM : PSKEL_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+void clear_error() { g_last_error.clear(); }
+
+// ---------------------------------------------------------- device context
+
+static std::mutex g_ctx_mu;
+static std::map<int, DeviceContext*> g_ctx;
+
+pskel_status get_context(DeviceContext** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  auto it = g_ctx.find(dev);
+  if (it != g_ctx.end()) {
+    *out = it->second;
+    return PSKEL_OK;
+  }
+  DeviceContext* c = new DeviceContext();
+  c->device = dev;
+  e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  e = cudaMalloc(&c->err, 64);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(error word)");
+  e = cudaMemset(c->err, 0, 64);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error word)");
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+  g_ctx[dev] = c;
+  *out = c;
+  return PSKEL_OK;
+}
+
+pskel_status ensure_buffer(DeviceBuffer& b, size_t bytes) {
+  if (b.bytes >= bytes && b.ptr) return PSKEL_OK;
+  if (b.ptr) cudaFree(b.ptr);
+  b.ptr = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaMalloc(&b.ptr, bytes ? bytes : 16);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(staging buffer)");
+  b.bytes = bytes;
+  return PSKEL_OK;
+}
+
+pskel_status device_sync_check(DeviceContext* c, cudaStream_t s) {
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  unsigned word = 0;
+  e = cudaMemcpy(&word, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
+  if (word) {
+    cudaMemset(c->err, 0, sizeof(unsigned));
+    std::string msg = "device error:";
+    if (word & kDevErrTimeout) msg += " a TMA/mbarrier wait timed out;";
+    if (word & kDevErrValue) msg += " a Life cell outside {0,1};";
+    if (word & kDevErrBarrier) msg += " a batched-schedule dependency wait timed out;";
+    return fail(PSKEL_ERR_DEVICE, "%s", msg.c_str());
+  }
+  return PSKEL_OK;
+}
+
+// ------------------------------------------------------------ tensor maps
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+cudaError_t encode_tmap(CUtensorMap* map, CUtensorMapDataType type, int rank, void* base, const uint64_t* dims,
+                        const uint64_t* strides_bytes, const uint32_t* box) {
+  if (!g_encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  cuuint64_t gd[3];
+  cuuint64_t gs[2];
+  cuuint32_t bx[3];
+  cuuint32_t es[3] = {1, 1, 1};
+  for (int i = 0; i < rank; ++i) {
+    gd[i] = dims[i];
+    bx[i] = box[i];
+  }
+  for (int i = 0; i + 1 < rank; ++i) gs[i] = strides_bytes[i];
+  CUresult r = g_encode(map, type, static_cast<cuuint32_t>(rank), base, gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+std::vector<int> plan_passes(int64_t iters, int T) {
+  std::vector<int> p;
+  if (iters <= 0) return p;
+  if (T < 1) T = 1;
+  for (int64_t k = 0; k < iters / T; ++k) p.push_back(T);
+  if (iters % T) p.push_back(static_cast<int>(iters % T));
+  if ((static_cast<int64_t>(p.size()) & 1) != (iters & 1)) {
+    // split the first pass of >= 2 steps in two
+    for (size_t i = 0; i < p.size(); ++i) {
+      if (p[i] >= 2) {
+        const int a = p[i] / 2, b = p[i] - a;
+        p[i] = a;
+        p.insert(p.begin() + static_cast<long>(i) + 1, b);
+        break;
+      }
+    }
+  }
+  return p;
+}
+
+// --------------------------------------------------------------- validation
+
+static size_t dtype_size(pskel_dtype d) { return d == PSKEL_U8 ? 1 : (d == PSKEL_F32 ? 4 : 2); }
+
+pskel_status check_mask(const pskel_mask& m, int dim, bool need_weights, int* max_off, int* ring) {
+  if (m.dimension != dim) return fail(PSKEL_ERR_INVALID, "mask dimension %d, expected %d", m.dimension, dim);
+  if (m.size < 1) return fail(PSKEL_ERR_INVALID, "mask has no entries");
+  if (!m.offsets) return fail(PSKEL_ERR_INVALID, "mask offsets pointer is NULL");
+  if (need_weights && !m.weights) return fail(PSKEL_ERR_INVALID, "mask weights pointer is NULL");
+  if (m.range < 0) return fail(PSKEL_ERR_INVALID, "negative mask range");
+  int R = 0;
+  for (int i = 0; i < m.size * dim; ++i) R = std::max(R, std::abs(m.offsets[i]));
+  int r = m.range > 0 ? m.range : R;
+  if (r < R)
+    return fail(PSKEL_ERR_INVALID,
+                "mask range %d is smaller than its largest offset %d: updated cells would read outside the grid", r, R);
+  *max_off = R;
+  *ring = r;
+  return PSKEL_OK;
+}
+
+static pskel_status check_life_mask(const pskel_mask& m) {
+  if (m.size != 8) return fail(PSKEL_ERR_UNSUPPORTED, "Life kernel needs the 8-entry Moore mask, got %d entries", m.size);
+  int seen = 0;
+  for (int n = 0; n < 8; ++n) {
+    const int dh = m.offsets[2 * n], dw = m.offsets[2 * n + 1];
+    if (dh < -1 || dh > 1 || dw < -1 || dw > 1 || (dh == 0 && dw == 0))
+      return fail(PSKEL_ERR_UNSUPPORTED, "Life kernel needs the Moore mask; entry %d is (%d,%d)", n, dh, dw);
+    const int bit = 1 << ((dh + 1) * 3 + (dw + 1));
+    if (seen & bit) return fail(PSKEL_ERR_UNSUPPORTED, "Life mask repeats offset (%d,%d)", dh, dw);
+    seen |= bit;
+  }
+  return PSKEL_OK;
+}
+
+static bool tma_ok(const void* p, int64_t pitch_bytes) {
+  return (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (pitch_bytes & 15) == 0 && pitch_bytes < (int64_t(1) << 40);
+}
+
+// ------------------------------------------------------------- 2D iterate
+
+static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
+                                 int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,
+                                 cudaStream_t s) {
+  LifeGeom g;
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : kLifeMaxT;
+  T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeMaxT), std::max<int64_t>(iters, 1)));
+  int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
+  TH = std::min(TH, 256 - 2 * T) & ~1;
+  if (TH < 2) return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", T);
+  g.T = T;
+  g.TH = TH;
+  g.LH = TH + 2 * T;
+  g.tiles_x = static_cast<int>((W + kLifeTW - 1) / kLifeTW);
+  g.tiles_y = static_cast<int>((H + TH - 1) / TH);
+  const int ntiles = g.tiles_x * g.tiles_y;
+  const int per_sm = life_max_ctas_per_sm(g.LH);
+  g.ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
+  g.ctas = std::max(1, std::min(g.ctas, ntiles));
+  const bool use_tma = tma_ok(in, pitch) && tma_ok(out, pitch);
+  CUtensorMap map_in, map_out;
+  memset(&map_in, 0, sizeof(map_in));
+  memset(&map_out, 0, sizeof(map_out));
+  if (use_tma) {
+    const uint64_t dims[2] = {static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
+    const uint64_t strides[1] = {static_cast<uint64_t>(pitch)};
+    const uint32_t box[2] = {static_cast<uint32_t>(kLifeLW), static_cast<uint32_t>(g.LH)};
+    cudaError_t e = encode_tmap(&map_in, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, in, dims, strides, box);
+    if (e == cudaSuccess) e = encode_tmap(&map_out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, out, dims, strides, box);
+    if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled");
+  }
+  const std::vector<int> passes = plan_passes(iters, T);
+  for (size_t i = 0; i < passes.size(); ++i) {
+    const bool fwd = (i % 2 == 0);
+    const uint8_t* src = static_cast<const uint8_t*>(fwd ? in : out);
+    uint8_t* dst = static_cast<uint8_t*>(fwd ? out : in);
+    cudaError_t e = life_pass(fwd ? &map_in : &map_out, use_tma, src, dst, static_cast<int>(W), static_cast<int>(H),
+                              pitch, ring, passes[i], g, c->err, s);
+    if (e != cudaSuccess) return cuda_fail(e, "Life kernel launch");
+  }
+  (void)st;
+  return PSKEL_OK;
+}
+
+static pskel_status iterate_float2d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
+                                    int64_t iters, int R, int ring, const pskel_schedule* sched, DeviceContext* c,
+                                    cudaStream_t s) {
+  const Op2D op = (st.op == PSKEL_OP_ADVECT) ? Op2D::Advect : Op2D::Linear;
+  const int dtype = static_cast<int>(st.dtype);
+  const size_t esz = dtype_size(st.dtype);
+  const int vec = static_cast<int>(16 / esz);
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : (op == Op2D::Advect ? 4 : 8);
+  T = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(iters, 1)));
+  if (R == 0) T = 1;  // a mask reaching no neighbour needs no halo
+  int TW = (sched && sched->tile_w > 0) ? sched->tile_w : (op == Op2D::Advect ? 64 : 128);
+  int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 64;
+  TW = std::max(vec, (TW / vec) * vec);
+  // shrink the temporal block until the halo tile fits a TMA box (<= 256 per side)
+  int HY = 0, HX = 0;
+  for (;;) {
+    HY = R * T;
+    HX = ((R * T + vec - 1) / vec) * vec;
+    if ((TW + 2 * HX <= 256 && TH + 2 * HY <= 256) || T == 1) break;
+    --T;
+  }
+  if (TW + 2 * HX > 256) TW = std::max(vec, ((256 - 2 * HX) / vec) * vec);
+  if (TH + 2 * HY > 256) TH = 256 - 2 * HY;
+  if (TW < vec || TH < 1 || TW + 2 * HX > 256 || TH + 2 * HY > 256)
+    return fail(PSKEL_ERR_UNSUPPORTED, "mask reach %d too large for the 2D tile kernel", R);
+  int LW = TW + 2 * HX, LH = TH + 2 * HY;
+  while (stencil2d_smem_bytes(op, dtype, LW, LH) > static_cast<size_t>(c->smem_optin) && TH > 8) {
+    TH /= 2;
+    LH = TH + 2 * HY;
+  }
+  if (stencil2d_smem_bytes(op, dtype, LW, LH) > static_cast<size_t>(c->smem_optin))
+    return fail(PSKEL_ERR_UNSUPPORTED, "2D tile does not fit in shared memory");
+
+  Stencil2DParams p;
+  memset(&p, 0, sizeof(p));
+  p.W = static_cast<int>(W);
+  p.H = static_cast<int>(H);
+  p.pitch = pitch;
+  p.ring = ring;
+  p.R = R;
+  p.T = T;
+  p.TW = TW;
+  p.TH = TH;
+  p.LW = LW;
+  p.LH = LH;
+  p.HX = HX;
+  p.HY = HY;
+  p.tiles_x = static_cast<int>((W + TW - 1) / TW);
+  p.tiles_y = static_cast<int>((H + TH - 1) / TH);
+  p.err = c->err;
+  if (op == Op2D::Linear) {
+    p.nm = st.mask.size;
+    for (int n = 0; n < p.nm; ++n) {
+      p.off[n] = st.mask.offsets[2 * n] * LW + st.mask.offsets[2 * n + 1];
+      p.wt[n] = st.mask.weights[n];
+    }
+  } else {
+    p.K = st.diffusivity;
+    p.dt = st.dt;
+    p.inv_dx = st.inv_dx;
+    p.u = st.wind_u;
+    p.v = st.wind_v;
+  }
+  const int ntiles = p.tiles_x * p.tiles_y;
+  const int per_sm = std::max(1, stencil2d_max_ctas_per_sm(op, dtype, p.nm, LW, LH));
+  int ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
+  ctas = std::max(1, std::min(ctas, ntiles));
+
+  const int64_t pitch_bytes = pitch * static_cast<int64_t>(esz);
+  bool use_tma = tma_ok(in, pitch_bytes) && tma_ok(out, pitch_bytes);
+  if (op == Op2D::Advect) use_tma = use_tma && tma_ok(st.wind_u, pitch_bytes) && tma_ok(st.wind_v, pitch_bytes);
+  CUtensorMap m_in, m_out, m_u, m_v;
+  memset(&m_in, 0, sizeof(m_in));
+  memset(&m_out, 0, sizeof(m_out));
+  memset(&m_u, 0, sizeof(m_u));
+  memset(&m_v, 0, sizeof(m_v));
+  if (use_tma) {
+    const CUtensorMapDataType tt = (dtype == PSKEL_BF16) ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const uint64_t dims[2] = {static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
+    const uint64_t strides[1] = {static_cast<uint64_t>(pitch_bytes)};
+    const uint32_t box[2] = {static_cast<uint32_t>(LW), static_cast<uint32_t>(LH)};
+    cudaError_t e = encode_tmap(&m_in, tt, 2, in, dims, strides, box);
+    if (e == cudaSuccess) e = encode_tmap(&m_out, tt, 2, out, dims, strides, box);
+    if (e == cudaSuccess && op == Op2D::Advect) {
+      e = encode_tmap(&m_u, tt, 2, const_cast<void*>(st.wind_u), dims, strides, box);
+      if (e == cudaSuccess) e = encode_tmap(&m_v, tt, 2, const_cast<void*>(st.wind_v), dims, strides, box);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled");
+  }
+  const std::vector<int> passes = plan_passes(iters, T);
+  for (size_t i = 0; i < passes.size(); ++i) {
+    const bool fwd = (i % 2 == 0);
+    p.src = fwd ? in : out;
+    p.dst = fwd ? out : in;
+    p.steps = passes[i];
+    cudaError_t e = stencil2d_pass(op, dtype, use_tma, fwd ? &m_in : &m_out, &m_u, &m_v, p, ctas, s);
+    if (e != cudaSuccess) return cuda_fail(e, "2D stencil kernel launch");
+  }
+  return PSKEL_OK;
+}
+
+pskel_status validate2d(const pskel_stencil* st, const void* in, const void* out, int64_t W, int64_t H, int64_t pitch,
+                        int64_t iters, int* R, int* ring) {
+  if (!st) return fail(PSKEL_ERR_INVALID, "stencil descriptor is NULL");
+  if (!in || !out) return fail(PSKEL_ERR_INVALID, "grid buffer pointer is NULL");
+  if (in == out) return fail(PSKEL_ERR_INVALID, "input and output must be distinct buffers");
+  if (W <= 0 || H <= 0) return fail(PSKEL_ERR_INVALID, "grid %lld x %lld is empty", (long long)W, (long long)H);
+  if (W >= (int64_t(1) << 31) || H >= (int64_t(1) << 31)) return fail(PSKEL_ERR_UNSUPPORTED, "grid side >= 2^31");
+  if (pitch < W) return fail(PSKEL_ERR_INVALID, "row pitch %lld is smaller than the width", (long long)pitch);
+  if (iters < 0) return fail(PSKEL_ERR_INVALID, "negative iteration count");
+  switch (st->op) {
+    case PSKEL_OP_LINEAR:
+      if (st->dtype != PSKEL_F32 && st->dtype != PSKEL_BF16)
+        return fail(PSKEL_ERR_UNSUPPORTED, "linear 2D stencil supports f32 and bf16 storage");
+      if (st->mask.size > kMaxMask2D) return fail(PSKEL_ERR_UNSUPPORTED, "2D mask larger than %d entries", kMaxMask2D);
+      if (pskel_status s = check_mask(st->mask, 2, true, R, ring)) return s;
+      break;
+    case PSKEL_OP_LIFE:
+      if (st->dtype != PSKEL_U8) return fail(PSKEL_ERR_UNSUPPORTED, "Life runs on uint8 cells");
+      if (pskel_status s = check_mask(st->mask, 2, false, R, ring)) return s;
+      if (pskel_status s = check_life_mask(st->mask)) return s;
+      break;
+    case PSKEL_OP_ADVECT:
+      if (st->dtype != PSKEL_F32 && st->dtype != PSKEL_BF16)
+        return fail(PSKEL_ERR_UNSUPPORTED, "advection supports f32 and bf16 storage");
+      if (!st->wind_u || !st->wind_v) return fail(PSKEL_ERR_INVALID, "advection wind field pointer is NULL");
+      if (st->mask.size > 0) {
+        if (pskel_status s = check_mask(st->mask, 2, false, R, ring)) return s;
+        if (*ring < 1) return fail(PSKEL_ERR_INVALID, "advection needs a ring of at least 1");
+      } else {
+        *ring = 1;
+      }
+      *R = 1;
+      break;
+    default:
+      return fail(PSKEL_ERR_INVALID, "unknown stencil op %d", static_cast<int>(st->op));
+  }
+  if (*R > 16) return fail(PSKEL_ERR_UNSUPPORTED, "mask reach %d > 16", *R);
+  if (H < *ring || W < *ring) return fail(PSKEL_ERR_INVALID, "grid smaller than the mask range");
+  return PSKEL_OK;
+}
+
+}  // namespace pskel
+
+using namespace pskel;
+
+extern "C" {
+
+int32_t pskel_version(void) { return 100; }
+
+const char* pskel_last_error(void) { return g_last_error.c_str(); }
+
+int32_t pskel_plan_passes(int64_t iterations, int32_t time_steps, int32_t* passes, int32_t cap) {
+  const std::vector<int> p = plan_passes(iterations, time_steps);
+  for (int32_t i = 0; i < cap && i < static_cast<int32_t>(p.size()); ++i) passes[i] = p[i];
+  return static_cast<int32_t>(p.size());
+}
+
+pskel_status pskel_sync(void* stream) {
+  clear_error();
+  DeviceContext* c = nullptr;
+  if (pskel_status s = get_context(&c)) return s;
+  return device_sync_check(c, static_cast<cudaStream_t>(stream));
+}
+
+pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height,
+                             int64_t pitch, int64_t iterations, const pskel_schedule* sched, void* stream) {
+  clear_error();
+  if (pitch == 0) pitch = width;
+  int R = 0, ring = 0;
+  if (pskel_status s = validate2d(st, in, out, width, height, pitch, iterations, &R, &ring)) return s;
+  if (iterations == 0) return PSKEL_OK;
+  DeviceContext* c = nullptr;
+  if (pskel_status s = get_context(&c)) return s;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (st->op == PSKEL_OP_LIFE) return iterate_life(*st, in, out, width, height, pitch, iterations, ring, sched, c, s);
+  return iterate_float2d(*st, in, out, width, height, pitch, iterations, R, ring, sched, c, s);
+}
+
+pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void* out_host, int64_t width,
+                              int64_t height, int64_t iterations, const pskel_schedule* sched) {
+  clear_error();
+  int R = 0, ring = 0;
+  if (!in_host || !out_host) return fail(PSKEL_ERR_INVALID, "host array pointer is NULL");
+  if (pskel_status s = validate2d(st, in_host, out_host, width, height, width, iterations, &R, &ring)) return s;
+  if (st->op == PSKEL_OP_ADVECT && (!st->wind_u || !st->wind_v))
+    return fail(PSKEL_ERR_INVALID, "advection wind field pointer is NULL");
+  DeviceContext* c = nullptr;
+  if (pskel_status s = get_context(&c)) return s;
+  const size_t esz = dtype_size(st->dtype);
+  const size_t row = static_cast<size_t>(width) * esz;
+  const size_t pitch_bytes = (row + 127) & ~size_t(127);
+  const size_t bytes = pitch_bytes * static_cast<size_t>(height);
+  const int64_t pitch = static_cast<int64_t>(pitch_bytes / esz);
+  if (pskel_status s = ensure_buffer(c->host_in, bytes)) return s;
+  if (pskel_status s = ensure_buffer(c->host_out, bytes)) return s;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaMemcpy2DAsync(c->host_in.ptr, pitch_bytes, in_host, row, row, height, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy input to device");
+  if (iterations % 2 == 1 && ring > 0) {
+    // the output array's ring is part of the result when the iteration count is odd
+    const uint8_t* oh = static_cast<const uint8_t*>(out_host);
+    uint8_t* od = static_cast<uint8_t*>(c->host_out.ptr);
+    const size_t r = static_cast<size_t>(std::min<int64_t>(ring, height));
+    e = cudaMemcpy2DAsync(od, pitch_bytes, oh, row, row, r, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && height > ring) {
+      const size_t top = static_cast<size_t>(height - r);
+      e = cudaMemcpy2DAsync(od + top * pitch_bytes, pitch_bytes, oh + top * row, row, row, r, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess && height > 2 * ring) {
+      const size_t mid = static_cast<size_t>(height - 2 * ring);
+      const size_t cw = std::min<size_t>(static_cast<size_t>(ring), static_cast<size_t>(width)) * esz;
+      e = cudaMemcpy2DAsync(od + r * pitch_bytes, pitch_bytes, oh + r * row, row, cw, mid, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess && width > ring) {
+        const size_t off = static_cast<size_t>(width - ring) * esz;
+        e = cudaMemcpy2DAsync(od + r * pitch_bytes + off, pitch_bytes, oh + r * row + off, row, cw, mid,
+                              cudaMemcpyHostToDevice, s);
+      }
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "copy output ring to device");
+  }
+  pskel_stencil dev = *st;
+  if (st->op == PSKEL_OP_ADVECT) {
+    if (pskel_status q = ensure_buffer(c->host_u, bytes)) return q;
+    if (pskel_status q = ensure_buffer(c->host_v, bytes)) return q;
+    e = cudaMemcpy2DAsync(c->host_u.ptr, pitch_bytes, st->wind_u, row, row, height, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(c->host_v.ptr, pitch_bytes, st->wind_v, row, row, height, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "copy wind fields to device");
+    dev.wind_u = c->host_u.ptr;
+    dev.wind_v = c->host_v.ptr;
+  }
+  if (pskel_status q = pskel_iterate2d(&dev, c->host_in.ptr, c->host_out.ptr, width, height, pitch, iterations, sched, s))
+    return q;
+  const void* result = (iterations % 2 == 1) ? c->host_out.ptr : c->host_in.ptr;
+  e = cudaMemcpy2DAsync(out_host, row, result, pitch_bytes, row, height, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy result to host");
+  return device_sync_check(c, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,34 @@
+// Host-side state and helpers shared by the C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pskel_gb300.h"
+
+namespace pskel {
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+// One per CUDA device, created on first use with that device current.
+struct DeviceContext {
+  int device = 0;
+  int sms = 0;
+  int smem_optin = 0;
+  unsigned* err = nullptr;        // device error word (kernels atomicOr into it)
+  cudaStream_t stream = nullptr;  // stream of the *_host entry points
+  DeviceBuffer host_in, host_out, host_u, host_v;  // staging for *_host
+};
+
+pskel_status fail(pskel_status code, const char* fmt, ...);
+pskel_status cuda_fail(cudaError_t e, const char* what);
+void clear_error();
+pskel_status get_context(DeviceContext** out);
+pskel_status ensure_buffer(DeviceBuffer& b, size_t bytes);
+pskel_status device_sync_check(DeviceContext* c, cudaStream_t s);
+pskel_status check_mask(const pskel_mask& m, int dim, bool need_weights, int* max_off, int* ring);
+
+}  // namespace pskel

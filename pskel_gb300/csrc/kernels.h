@@ -1,0 +1,83 @@
+// Internal launch interface between the C ABI (capi.cu) and the kernels.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace pskel {
+
+// Encodes a tiled tensor map through the driver entry point (no libcuda link).
+// rank 2: dims {W, H}, row stride in bytes; rank 3 adds the third dimension.
+cudaError_t encode_tmap(CUtensorMap* map, CUtensorMapDataType type, int rank, void* base, const uint64_t* dims,
+                        const uint64_t* strides_bytes, const uint32_t* box);
+
+// Splits `iters` steps into passes of at most `T` steps whose count has the
+// parity of `iters`, so a ping-pong over the passes ends in the buffer a
+// step-by-step ping-pong would end in.
+std::vector<int> plan_passes(int64_t iters, int T);
+
+// ------------------------------------------------------------------ Life
+
+struct LifeGeom {
+  int T;      // max steps per pass (halo rows), <= 16
+  int TH;     // core rows per tile
+  int LH;     // loaded rows per tile = TH + 2T (<= 256, even)
+  int tiles_x, tiles_y;
+  int ctas;
+};
+
+constexpr int kLifeLW = 256;                 // loaded bytes per tile row (TMA box width)
+constexpr int kLifeHX = 16;                  // horizontal halo, bytes
+constexpr int kLifeTW = kLifeLW - 2 * kLifeHX;  // 224 core columns
+constexpr int kLifeMaxT = 16;
+constexpr int kLifeThreads = 256;
+
+size_t life_smem_bytes(int LH);
+// One pass of `steps` (<= geom.T) Life steps from src to dst.
+cudaError_t life_pass(const CUtensorMap* map_src, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
+                      int64_t pitch, int ring, int steps, const LifeGeom& g, unsigned* err, cudaStream_t s);
+int life_max_ctas_per_sm(int LH);
+
+// ------------------------------------------------------- 2D float stencils
+
+enum class Op2D { Linear, Advect };
+
+constexpr int kMaxMask2D = 32;
+constexpr int kStencil2DThreads = 256;
+
+struct Stencil2DParams {
+  int W, H;
+  int64_t pitch;
+  int ring;        // r: cells with r <= h < H-r, r <= w < W-r are updated
+  int R;           // max |offset|: halo per step
+  int steps;       // steps in this pass
+  int T;           // geometry steps (halo = R*T rows)
+  int TW, TH;      // core tile
+  int LW, LH;      // loaded tile
+  int HX, HY;      // horizontal / vertical halo
+  int tiles_x, tiles_y;
+  int nm;                 // linear: mask size
+  int off[kMaxMask2D];    // linear: dh*LW + dw per entry
+  float wt[kMaxMask2D];   // linear: weights
+  float K, dt, inv_dx;    // advect
+  const void* src;
+  void* dst;
+  const void* u;
+  const void* v;
+  unsigned* err;
+};
+
+struct Stencil2DGeom {
+  int T, TW, TH, LW, LH, HX, HY, tiles_x, tiles_y, ctas;
+};
+
+// dtype: 1 = f32, 2 = bf16 (pskel_dtype values).
+size_t stencil2d_smem_bytes(Op2D op, int dtype, int LW, int LH);
+int stencil2d_max_ctas_per_sm(Op2D op, int dtype, int nm, int LW, int LH);
+cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* map_src, const CUtensorMap* map_u,
+                           const CUtensorMap* map_v, const Stencil2DParams& p, int ctas, cudaStream_t s);
+
+}  // namespace pskel

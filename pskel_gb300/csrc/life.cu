@@ -1,0 +1,246 @@
+// Game of Life, temporally blocked and bit-sliced.
+//
+// One pass advances the whole grid by up to 16 steps. Each persistent CTA
+// walks tiles of 224 x TH core cells: it stages the (TH + 2T) x 256 byte halo
+// tile into shared memory with one TMA load, packs the 0/1 bytes into 32-cell
+// bit words, runs the steps on the bit planes (neighbour counts with
+// bit-sliced full adders; one word = 32 cells per ~15 integer ops), then
+// unpacks the core and writes it with 128-bit coalesced stores. Ring cells
+// (outside r <= h < H-r, r <= w < W-r) are never updated and never written,
+// the semantics of Stencil2D::runOpenMP (PSkelStencil.hpp:2197-2257) that the
+// reference's GPU kernel also follows (guard at PSkelStencil.hpp:576).
+//
+// Redundant halo work: the tile carries T rows and 16 columns of halo on each
+// side; garbage entering from the tile edge advances one cell per step, so
+// the core is exact after T <= 16 steps.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pskel {
+namespace {
+
+constexpr int kWords = kLifeLW / 32;  // 8 bit words per tile row
+constexpr int kBitPitch = 9;          // padded: 8-row strips land on distinct banks
+
+// 16 cells (one byte each, value 0/1) -> 16 bits, cell i at bit i.
+__device__ __forceinline__ uint32_t pack16(uint4 v) {
+  const uint32_t n0 = (v.x * 0x01020408u) >> 24;
+  const uint32_t n1 = (v.y * 0x01020408u) >> 24;
+  const uint32_t n2 = (v.z * 0x01020408u) >> 24;
+  const uint32_t n3 = (v.w * 0x01020408u) >> 24;
+  return n0 | (n1 << 4) | (n2 << 8) | (n3 << 12);
+}
+
+// 16 bits -> 16 bytes of 0/1.
+__device__ __forceinline__ uint4 unpack16(uint32_t h) {
+  uint4 v;
+  v.x = ((h & 0xFu) * 0x00204081u) & 0x01010101u;
+  v.y = (((h >> 4) & 0xFu) * 0x00204081u) & 0x01010101u;
+  v.z = (((h >> 8) & 0xFu) * 0x00204081u) & 0x01010101u;
+  v.w = (((h >> 12) & 0xFu) * 0x00204081u) & 0x01010101u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t bit_range(int lo, int hi) {
+  lo = max(0, min(32, lo));
+  hi = max(0, min(32, hi));
+  if (hi <= lo) return 0u;
+  const uint32_t upto_hi = (hi == 32) ? 0xFFFFFFFFu : ((1u << hi) - 1u);
+  const uint32_t below_lo = (lo == 32) ? 0xFFFFFFFFu : ((1u << lo) - 1u);
+  return upto_hi & ~below_lo;
+}
+
+struct RowSums {
+  uint32_t c;       // the row's own cells
+  uint32_t t0, t1;  // west + centre + east, 2-bit sliced
+  uint32_t p0, p1;  // west + east, 2-bit sliced
+};
+
+__device__ __forceinline__ RowSums row_sums(const uint32_t* row, int j) {
+  RowSums r;
+  const uint32_t c = row[j];
+  const uint32_t l = (j > 0) ? row[j - 1] : 0u;
+  const uint32_t e = (j < kWords - 1) ? row[j + 1] : 0u;
+  const uint32_t we = __funnelshift_l(l, c, 1);  // bit b = cell b-1
+  const uint32_t ea = __funnelshift_r(c, e, 1);  // bit b = cell b+1
+  r.c = c;
+  r.t0 = we ^ c ^ ea;
+  r.t1 = (we & c) | (we & ea) | (c & ea);
+  r.p0 = we ^ ea;
+  r.p1 = we & ea;
+  return r;
+}
+
+__device__ __forceinline__ RowSums zero_row() {
+  RowSums r;
+  r.c = r.t0 = r.t1 = r.p0 = r.p1 = 0u;
+  return r;
+}
+
+template <bool kTma>
+__global__ void __launch_bounds__(kLifeThreads, 2)
+    life_kernel(const __grid_constant__ CUtensorMap map, const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                int W, int H, int64_t pitch, int ring, int steps, int T, int TH, int LH, int tiles_x, int tiles_y,
+                unsigned* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* bytes = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  uint32_t* bitsA = reinterpret_cast<uint32_t*>(bytes + LH * kLifeLW);
+  uint32_t* bitsB = bitsA + LH * kBitPitch;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(bitsB + LH * kBitPitch + ((LH * kBitPitch) & 1));
+
+  const int tid = threadIdx.x;
+  if (kTma && tid == 0) {
+    mbar_init(bar, 1);
+    fence_barrier_init();
+    prefetch_tensormap(&map);
+  }
+  __syncthreads();
+
+  uint32_t phase = 0;
+  bool bad_value = false;
+  const int ntiles = tiles_x * tiles_y;
+  const int j = tid & (kWords - 1);
+  const int strip = tid >> 3;                 // 32 strips of rows
+  const int rps = (LH + 31) >> 5;             // rows per strip
+  const int ya = strip * rps;
+  const int yb = min(LH, ya + rps);
+
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int ty = tile / tiles_x;
+    const int tx = tile - ty * tiles_x;
+    const int gy0 = ty * TH - T;          // global row of local row 0
+    const int gx0 = tx * kLifeTW - kLifeHX;  // global column of local column 0
+
+    // ---- stage the halo tile
+    if (kTma) {
+      if (tid == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, static_cast<uint32_t>(LH * kLifeLW));
+        tma_load_2d(bytes, &map, gx0, gy0, bar);
+      }
+      if (!mbar_wait_bounded(bar, phase, err)) return;
+      phase ^= 1u;
+    } else {
+      for (int i = tid; i < LH * 16; i += kLifeThreads) {
+        const int row = i >> 4, c = i & 15;
+        const int gy = gy0 + row, gx = gx0 + c * 16;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (gy >= 0 && gy < H) {
+          const uint8_t* p = src + static_cast<int64_t>(gy) * pitch + gx;
+          if (gx >= 0 && gx + 16 <= W && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+            v = *reinterpret_cast<const uint4*>(p);
+          } else {
+            uint8_t tmp[16];
+#pragma unroll
+            for (int b = 0; b < 16; ++b) tmp[b] = (gx + b >= 0 && gx + b < W) ? p[b] : 0;
+            v.x = tmp[0] | (tmp[1] << 8) | (tmp[2] << 16) | (uint32_t(tmp[3]) << 24);
+            v.y = tmp[4] | (tmp[5] << 8) | (tmp[6] << 16) | (uint32_t(tmp[7]) << 24);
+            v.z = tmp[8] | (tmp[9] << 8) | (tmp[10] << 16) | (uint32_t(tmp[11]) << 24);
+            v.w = tmp[12] | (tmp[13] << 8) | (tmp[14] << 16) | (uint32_t(tmp[15]) << 24);
+          }
+        }
+        *reinterpret_cast<uint4*>(bytes + row * kLifeLW + c * 16) = v;
+      }
+      __syncthreads();
+    }
+
+    // ---- bytes -> bit words (LH is even, so each warp's trip count is uniform)
+    for (int i = tid; i < LH * 16; i += kLifeThreads) {
+      const int row = i >> 4, c = i & 15;
+      const uint4 v = *reinterpret_cast<const uint4*>(bytes + row * kLifeLW + c * 16);
+      if ((v.x | v.y | v.z | v.w) & 0xFEFEFEFEu) bad_value = true;
+      const uint32_t half = pack16(v);
+      const uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, half, 1);
+      if ((c & 1) == 0) bitsA[row * kBitPitch + (c >> 1)] = half | (other << 16);
+    }
+    __syncthreads();
+
+    // ---- the steps, on bit planes
+    const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
+    for (int s = 0; s < steps; ++s) {
+      const uint32_t* in = (s & 1) ? bitsB : bitsA;
+      uint32_t* out = (s & 1) ? bitsA : bitsB;
+      if (ya < yb) {
+        RowSums prev = (ya > 0) ? row_sums(in + (ya - 1) * kBitPitch, j) : zero_row();
+        RowSums cur = row_sums(in + ya * kBitPitch, j);
+        for (int y = ya; y < yb; ++y) {
+          const RowSums next = (y + 1 < LH) ? row_sums(in + (y + 1) * kBitPitch, j) : zero_row();
+          // neighbour count = prev(w,c,e) + cur(w,e) + next(w,c,e), kept mod 8
+          const uint32_t s0 = prev.t0 ^ cur.p0 ^ next.t0;
+          const uint32_t k0 = (prev.t0 & cur.p0) | (prev.t0 & next.t0) | (cur.p0 & next.t0);
+          const uint32_t x1 = prev.t1 ^ cur.p1 ^ next.t1;
+          const uint32_t y1 = (prev.t1 & cur.p1) | (prev.t1 & next.t1) | (cur.p1 & next.t1);
+          const uint32_t s1 = x1 ^ k0;
+          const uint32_t s2 = y1 ^ (x1 & k0);
+          const uint32_t alive = s1 & ~s2 & (s0 | cur.c);  // count 3, or count 2 and alive
+          const int gy = gy0 + y;
+          const uint32_t m = (gy >= ring && gy < H - ring) ? colmask : 0u;
+          out[y * kBitPitch + j] = (alive & m) | (cur.c & ~m);
+          prev = cur;
+          cur = next;
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- core bits -> bytes -> global (interior cells only)
+    const uint32_t* fin = (steps & 1) ? bitsB : bitsA;
+    for (int i = tid; i < TH * 16; i += kLifeThreads) {
+      const int c = i & 15;
+      if (c == 0 || c == 15) continue;
+      const int row = T + (i >> 4);
+      const int gy = gy0 + row;
+      if (gy < ring || gy >= H - ring) continue;
+      const int gx = gx0 + c * 16;
+      if (gx + 16 <= ring || gx >= W - ring) continue;
+      const uint32_t word = fin[row * kBitPitch + (c >> 1)];
+      const uint4 v = unpack16((c & 1) ? (word >> 16) : (word & 0xFFFFu));
+      uint8_t* d = dst + static_cast<int64_t>(gy) * pitch + gx;
+      if (gx >= ring && gx + 16 <= W - ring && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+        *reinterpret_cast<uint4*>(d) = v;
+      } else {
+        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int b = 0; b < 16; ++b) {
+          const int x = gx + b;
+          if (x >= ring && x < W - ring) d[b] = static_cast<uint8_t>(w4[b >> 2] >> ((b & 3) * 8));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (bad_value) atomicOr(err, kDevErrValue);
+}
+
+}  // namespace
+
+size_t life_smem_bytes(int LH) {
+  return 128 + static_cast<size_t>(LH) * kLifeLW + 2 * static_cast<size_t>(LH) * kBitPitch * 4 + 16;
+}
+
+int life_max_ctas_per_sm(int LH) {
+  int n = 0;
+  const size_t smem = life_smem_bytes(LH);
+  cudaFuncSetAttribute(life_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaFuncSetAttribute(life_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_kernel<true>, kLifeThreads, smem) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t life_pass(const CUtensorMap* map_src, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
+                      int64_t pitch, int ring, int steps, const LifeGeom& g, unsigned* err, cudaStream_t s) {
+  const size_t smem = life_smem_bytes(g.LH);
+  CUtensorMap dummy;
+  if (!use_tma) memset(&dummy, 0, sizeof(dummy));
+  const CUtensorMap& m = use_tma ? *map_src : dummy;
+  if (use_tma) {
+    life_kernel<true><<<g.ctas, kLifeThreads, smem, s>>>(m, src, dst, W, H, pitch, ring, steps, g.T, g.TH, g.LH,
+                                                         g.tiles_x, g.tiles_y, err);
+  } else {
+    life_kernel<false><<<g.ctas, kLifeThreads, smem, s>>>(m, src, dst, W, H, pitch, ring, steps, g.T, g.TH, g.LH,
+                                                          g.tiles_x, g.tiles_y, err);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace pskel

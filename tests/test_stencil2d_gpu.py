@@ -1,0 +1,169 @@
+"""2D fp32 / bf16-storage stencils on the GPU against the oracle.
+
+fp32 results are compared bit for bit (same operation order, no contraction),
+which is stricter than the 1e-6 max relative error bar; bf16-storage results
+are compared bit for bit against the oracle's bf16 restatement. Every float
+case also reports its error against the fp64 oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import pskel_gb300 as P
+from pskel_gb300 import synth as S
+from tests.golden.make_golden import STAR9_OFFSETS, STAR9_WEIGHTS
+from tests.gpu_util import bits, run2d
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL_F32 = 1e-6  # fp32 parity bar; the kernels are expected to be bit-exact
+
+
+def max_rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)))
+
+
+def jac_grids(W, H, seed, dtype):
+    a, b = S.jacobi2d(W, H, seed=seed)
+    b = b.copy()
+    b[0, :] = 0.5
+    b[:, -1] = 0.25
+    if dtype == "bf16":
+        return S.f32_to_bf16(a), S.f32_to_bf16(b)
+    return a, b
+
+
+def sched(T=0, tw=0, th=0, ctas=0):
+    return dict(time_steps=T, tile_w=tw, tile_h=th, tile_d=0, ctas=ctas)
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H", [(37, 29), (130, 67), (1024, 1024), (1, 1), (5, 300), (257, 3)])
+@pytest.mark.parametrize("iters", [1, 2, 9])
+def test_jacobi_matches_oracle(cuda, oracle_mod, dtype, W, H, iters):
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    a, b = jac_grids(W, H, W + H, dtype)
+    got = run2d(cuda, st, a, b, iters, dtype=dtype)
+    want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("T,tw,th", [(1, 0, 0), (3, 32, 16), (8, 128, 64), (16, 64, 100), (5, 8, 1)])
+def test_jacobi_schedules(cuda, oracle_mod, dtype, T, tw, th):
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    a, b = jac_grids(301, 203, 5, dtype)
+    got = run2d(cuda, st, a, b, 23, sched=sched(T, tw, th), dtype=dtype)
+    want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, 23, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("offsets,weights", [
+    (STAR9_OFFSETS, STAR9_WEIGHTS),                                   # radius 2, 9 entries
+    ([(0, 0), (-1, -1), (1, 1), (-3, 2), (2, -1), (0, 3)],            # 6 entries: runtime-size path
+     [0.3, 0.1, 0.2, 0.15, 0.05, 0.2]),
+    ([(0, 0)], [0.5]),                                                # no neighbour at all
+])
+def test_general_masks_f32(cuda, oracle_mod, offsets, weights):
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "f32", offsets, weights, keep=keep)
+    a = S.uniform_f32(3, 1, (97, 211))
+    b = S.uniform_f32(3, 2, (97, 211))
+    for iters in (1, 4, 11):
+        got = run2d(cuda, st, a, b, iters)
+        want = oracle_mod.lin2d(a, b, offsets, weights, iters)
+        assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("pitch", [131, 136, 256])
+def test_pitched_rows(cuda, oracle_mod, dtype, pitch):
+    # 131 * elem is not 16-byte aligned: the tile is staged without TMA
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    a, b = jac_grids(129, 77, 2, dtype)
+    got = run2d(cuda, st, a, b, 13, pitch=pitch, dtype=dtype)
+    want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, 13, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))
+
+
+def _advect_inputs(W, H, seed, dtype):
+    a, b, u, v = S.advect2d(W, H, seed=seed)
+    b = b.copy()
+    b[-1, :] = 0.75
+    if dtype == "bf16":
+        return [S.f32_to_bf16(x) for x in (a, b, u, v)]
+    return a, b, u, v
+
+
+def _advect_gpu(torch, dtype, a, b, u, v, iters, sch=None):
+    from tests.gpu_util import np_view, to_dev
+    ud = to_dev(torch, np_view(u, dtype))
+    vd = to_dev(torch, np_view(v, dtype))
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_ADVECT, dtype, S.JACOBI4_OFFSETS, wind=(ud.data_ptr(), vd.data_ptr()), K=S.ADVECT_K,
+                        dt=S.ADVECT_DT, inv_dx=S.ADVECT_INV_DX, keep=keep)
+    return run2d(torch, st, a, b, iters, sched=sch, dtype=dtype)
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H,iters", [(40, 33, 9), (300, 211, 16), (64, 64, 1)])
+def test_advection_matches_oracle(cuda, oracle_mod, dtype, W, H, iters):
+    a, b, u, v = _advect_inputs(W, H, W, dtype)
+    got = _advect_gpu(cuda, dtype, a, b, u, v, iters)
+    want = oracle_mod.advect(a, b, u, v, iters, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("T", [1, 2, 6])
+def test_advection_schedules(cuda, oracle_mod, T):
+    a, b, u, v = _advect_inputs(257, 190, 4, "f32")
+    got = _advect_gpu(cuda, "f32", a, b, u, v, 14, sch=sched(T, 32, 24))
+    want = oracle_mod.advect(a, b, u, v, 14, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX)
+    assert np.array_equal(bits(got), bits(want))
+
+
+def test_host_entry_point_jacobi(cuda, oracle_mod):
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    for iters in (0, 1, 4, 7):
+        a, b = jac_grids(333, 251, iters, "f32")
+        a0, out = a.copy(), b.copy()
+        P.run2d_host(st, a, out, iters)
+        assert np.array_equal(bits(out), bits(oracle_mod.lin2d(a0, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters)))
+        assert np.array_equal(a, a0)
+
+
+def test_host_entry_point_advection_bf16(cuda, oracle_mod):
+    a, b, u, v = _advect_inputs(190, 170, 8, "bf16")
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_ADVECT, "bf16", S.JACOBI4_OFFSETS, wind=(u.ctypes.data, v.ctypes.data), K=S.ADVECT_K,
+                        dt=S.ADVECT_DT, inv_dx=S.ADVECT_INV_DX, keep=keep)
+    out = b.copy()
+    P.run2d_host(st, a, out, 5)
+    want = oracle_mod.advect(a, b, u, v, 5, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype="bf16")
+    assert np.array_equal(out, want)
+
+
+def test_jacobi_c1_full_size_and_fp64_error(cuda, oracle_mod):
+    # 1024^2, 100 iterations: bit-exact against the fp32 oracle; the fp32 and
+    # bf16-storage errors against the fp64 oracle are reported.
+    keep = P._Keep()
+    a, b = S.jacobi2d(1024, 1024, seed=1)
+    st = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    got = run2d(cuda, st, a, b, 100)
+    want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, 100)
+    assert np.array_equal(bits(got), bits(want))
+    ref64 = oracle_mod.lin2d(a.astype(np.float64), b.astype(np.float64), S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, 100,
+                             dtype="f64")
+    err32 = float(np.max(np.abs(got - ref64)))
+    stb = P.make_stencil(P.OP_LINEAR, "bf16", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    gb = run2d(cuda, stb, S.f32_to_bf16(a), S.f32_to_bf16(b), 100, dtype="bf16")
+    errb = float(np.max(np.abs(S.bf16_to_f32(gb) - ref64)))
+    print(f"\njacobi 1024^2 x100: max abs error vs fp64: fp32 {err32:.3e}, bf16 storage {errb:.3e}")
+    assert err32 < 1e-5 and errb < 2e-2

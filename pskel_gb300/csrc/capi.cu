@@ -223,7 +223,7 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
     const bool fwd = (i % 2 == 0);
     const uint8_t* src = static_cast<const uint8_t*>(fwd ? in : out);
     uint8_t* dst = static_cast<uint8_t*>(fwd ? out : in);
-    cudaError_t e = life_pass(fwd ? &map_in : &map_out, use_tma, src, dst, static_cast<int>(W), static_cast<int>(H),
+    cudaError_t e = life_pass(fwd ? &map_in : &map_out, fwd ? &map_out : &map_in, use_tma, src, dst, static_cast<int>(W), static_cast<int>(H),
                               pitch, ring, passes[i], g, c->err, s);
     if (e != cudaSuccess) return cuda_fail(e, "Life kernel launch");
   }
@@ -326,7 +326,8 @@ static pskel_status iterate_float2d(const pskel_stencil& st, void* in, void* out
     p.src = fwd ? in : out;
     p.dst = fwd ? out : in;
     p.steps = passes[i];
-    cudaError_t e = stencil2d_pass(op, dtype, use_tma, fwd ? &m_in : &m_out, &m_u, &m_v, p, ctas, s);
+    cudaError_t e = stencil2d_pass(op, dtype, use_tma, fwd ? &m_in : &m_out, fwd ? &m_out : &m_in, &m_u, &m_v, p,
+                                   ctas, s);
     if (e != cudaSuccess) return cuda_fail(e, "2D stencil kernel launch");
   }
   return PSKEL_OK;

@@ -37,7 +37,7 @@ constexpr int kLifeThreads = 256;
 
 size_t life_smem_bytes(int LH);
 // One pass of `steps` (<= geom.T) Life steps from src to dst.
-cudaError_t life_pass(const CUtensorMap* map_src, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
+cudaError_t life_pass(const CUtensorMap* map_src, const CUtensorMap* map_dst, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
                       int64_t pitch, int ring, int steps, const LifeGeom& g, unsigned* err, cudaStream_t s);
 int life_max_ctas_per_sm(int LH);
 
@@ -77,7 +77,8 @@ struct Stencil2DGeom {
 // dtype: 1 = f32, 2 = bf16 (pskel_dtype values).
 size_t stencil2d_smem_bytes(Op2D op, int dtype, int LW, int LH);
 int stencil2d_max_ctas_per_sm(Op2D op, int dtype, int nm, int LW, int LH);
-cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* map_src, const CUtensorMap* map_u,
+cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* map_src, const CUtensorMap* map_dst,
+                           const CUtensorMap* map_u,
                            const CUtensorMap* map_v, const Stencil2DParams& p, int ctas, cudaStream_t s);
 
 }  // namespace pskel

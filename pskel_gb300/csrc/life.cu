@@ -79,7 +79,8 @@ __device__ __forceinline__ RowSums zero_row() {
 
 template <bool kTma>
 __global__ void __launch_bounds__(kLifeThreads, 2)
-    life_kernel(const __grid_constant__ CUtensorMap map, const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+    life_kernel(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map_dst,
+                const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
                 int W, int H, int64_t pitch, int ring, int steps, int T, int TH, int LH, int tiles_x, int tiles_y,
                 unsigned* err) {
   extern __shared__ uint8_t smem_raw[];
@@ -93,6 +94,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
     mbar_init(bar, 1);
     fence_barrier_init();
     prefetch_tensormap(&map);
+    prefetch_tensormap(&map_dst);
   }
   __syncthreads();
 
@@ -111,47 +113,73 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
     const int gy0 = ty * TH - T;          // global row of local row 0
     const int gx0 = tx * kLifeTW - kLifeHX;  // global column of local column 0
 
-    // ---- stage the halo tile
-    if (kTma) {
-      if (tid == 0) {
-        fence_proxy_async();
-        mbar_arrive_expect_tx(bar, static_cast<uint32_t>(LH * kLifeLW));
-        tma_load_2d(bytes, &map, gx0, gy0, bar);
+    // Ring cells (outside r <= h < H-r, r <= w < W-r) are never written, so
+    // each global buffer keeps its own ring and step k reads the ring of the
+    // buffer it reads from. Tiles that reach the ring therefore also stage the
+    // destination buffer: its ring is what the odd steps of the pass read.
+    const bool touches_ring = (gy0 < ring) || (gy0 + LH > H - ring) || (gx0 < ring) || (gx0 + kLifeLW > W - ring);
+    const int nstage = (touches_ring && steps >= 2) ? 2 : 1;
+    for (int k = 0; k < nstage; ++k) {
+      if (k == 1) __syncthreads();  // the byte tile is reused
+      if (kTma) {
+        if (tid == 0) {
+          fence_proxy_async();
+          mbar_arrive_expect_tx(bar, static_cast<uint32_t>(LH * kLifeLW));
+          tma_load_2d(bytes, k == 0 ? &map : &map_dst, gx0, gy0, bar);
+        }
+        if (!mbar_wait_bounded(bar, phase, err)) return;
+        phase ^= 1u;
+      } else {
+        const uint8_t* from = (k == 0) ? src : dst;
+        for (int i = tid; i < LH * 16; i += kLifeThreads) {
+          const int row = i >> 4, c = i & 15;
+          const int gy = gy0 + row, gx = gx0 + c * 16;
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (gy >= 0 && gy < H) {
+            const uint8_t* p = from + static_cast<int64_t>(gy) * pitch + gx;
+            if (gx >= 0 && gx + 16 <= W && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+              v = *reinterpret_cast<const uint4*>(p);
+            } else {
+              uint8_t tmp[16];
+#pragma unroll
+              for (int b = 0; b < 16; ++b) tmp[b] = (gx + b >= 0 && gx + b < W) ? p[b] : 0;
+              v.x = tmp[0] | (tmp[1] << 8) | (tmp[2] << 16) | (uint32_t(tmp[3]) << 24);
+              v.y = tmp[4] | (tmp[5] << 8) | (tmp[6] << 16) | (uint32_t(tmp[7]) << 24);
+              v.z = tmp[8] | (tmp[9] << 8) | (tmp[10] << 16) | (uint32_t(tmp[11]) << 24);
+              v.w = tmp[12] | (tmp[13] << 8) | (tmp[14] << 16) | (uint32_t(tmp[15]) << 24);
+            }
+          }
+          *reinterpret_cast<uint4*>(bytes + row * kLifeLW + c * 16) = v;
+        }
+        __syncthreads();
       }
-      if (!mbar_wait_bounded(bar, phase, err)) return;
-      phase ^= 1u;
-    } else {
+      // bytes -> bit words (LH is even, so each warp's trip count is uniform)
+      uint32_t* plane = (k == 0) ? bitsA : bitsB;
       for (int i = tid; i < LH * 16; i += kLifeThreads) {
         const int row = i >> 4, c = i & 15;
-        const int gy = gy0 + row, gx = gx0 + c * 16;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (gy >= 0 && gy < H) {
-          const uint8_t* p = src + static_cast<int64_t>(gy) * pitch + gx;
-          if (gx >= 0 && gx + 16 <= W && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
-            v = *reinterpret_cast<const uint4*>(p);
+        uint4 v = *reinterpret_cast<const uint4*>(bytes + row * kLifeLW + c * 16);
+        if ((v.x | v.y | v.z | v.w) & 0xFEFEFEFEu) {
+          if (k == 0) {
+            bad_value = true;  // every source cell is state
           } else {
-            uint8_t tmp[16];
-#pragma unroll
-            for (int b = 0; b < 16; ++b) tmp[b] = (gx + b >= 0 && gx + b < W) ? p[b] : 0;
-            v.x = tmp[0] | (tmp[1] << 8) | (tmp[2] << 16) | (uint32_t(tmp[3]) << 24);
-            v.y = tmp[4] | (tmp[5] << 8) | (tmp[6] << 16) | (uint32_t(tmp[7]) << 24);
-            v.z = tmp[8] | (tmp[9] << 8) | (tmp[10] << 16) | (uint32_t(tmp[11]) << 24);
-            v.w = tmp[12] | (tmp[13] << 8) | (tmp[14] << 16) | (uint32_t(tmp[15]) << 24);
+            // only the destination's ring is read; its interior may hold anything
+            const int gy = gy0 + row, gx = gx0 + c * 16;
+            const bool row_ring = (gy < ring) || (gy >= H - ring);
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+            for (int b = 0; b < 16; ++b) {
+              const uint32_t byte = (w4[b >> 2] >> ((b & 3) * 8)) & 0xFFu;
+              if (byte > 1u && (row_ring || gx + b < ring || gx + b >= W - ring)) bad_value = true;
+            }
           }
+          v.x &= 0x01010101u;
+          v.y &= 0x01010101u;
+          v.z &= 0x01010101u;
+          v.w &= 0x01010101u;
         }
-        *reinterpret_cast<uint4*>(bytes + row * kLifeLW + c * 16) = v;
+        const uint32_t half = pack16(v);
+        const uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, half, 1);
+        if ((c & 1) == 0) plane[row * kBitPitch + (c >> 1)] = half | (other << 16);
       }
-      __syncthreads();
-    }
-
-    // ---- bytes -> bit words (LH is even, so each warp's trip count is uniform)
-    for (int i = tid; i < LH * 16; i += kLifeThreads) {
-      const int row = i >> 4, c = i & 15;
-      const uint4 v = *reinterpret_cast<const uint4*>(bytes + row * kLifeLW + c * 16);
-      if ((v.x | v.y | v.z | v.w) & 0xFEFEFEFEu) bad_value = true;
-      const uint32_t half = pack16(v);
-      const uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, half, 1);
-      if ((c & 1) == 0) bitsA[row * kBitPitch + (c >> 1)] = half | (other << 16);
     }
     __syncthreads();
 
@@ -175,7 +203,8 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
           const uint32_t alive = s1 & ~s2 & (s0 | cur.c);  // count 3, or count 2 and alive
           const int gy = gy0 + y;
           const uint32_t m = (gy >= ring && gy < H - ring) ? colmask : 0u;
-          out[y * kBitPitch + j] = (alive & m) | (cur.c & ~m);
+          uint32_t* o = out + y * kBitPitch + j;
+          *o = (m == 0xFFFFFFFFu) ? alive : ((alive & m) | (*o & ~m));
           prev = cur;
           cur = next;
         }
@@ -227,17 +256,18 @@ int life_max_ctas_per_sm(int LH) {
   return n > 0 ? n : 1;
 }
 
-cudaError_t life_pass(const CUtensorMap* map_src, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
+cudaError_t life_pass(const CUtensorMap* map_src, const CUtensorMap* map_dst, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
                       int64_t pitch, int ring, int steps, const LifeGeom& g, unsigned* err, cudaStream_t s) {
   const size_t smem = life_smem_bytes(g.LH);
   CUtensorMap dummy;
-  if (!use_tma) memset(&dummy, 0, sizeof(dummy));
+  memset(&dummy, 0, sizeof(dummy));
   const CUtensorMap& m = use_tma ? *map_src : dummy;
+  const CUtensorMap& md = use_tma ? *map_dst : dummy;
   if (use_tma) {
-    life_kernel<true><<<g.ctas, kLifeThreads, smem, s>>>(m, src, dst, W, H, pitch, ring, steps, g.T, g.TH, g.LH,
+    life_kernel<true><<<g.ctas, kLifeThreads, smem, s>>>(m, md, src, dst, W, H, pitch, ring, steps, g.T, g.TH, g.LH,
                                                          g.tiles_x, g.tiles_y, err);
   } else {
-    life_kernel<false><<<g.ctas, kLifeThreads, smem, s>>>(m, src, dst, W, H, pitch, ring, steps, g.T, g.TH, g.LH,
+    life_kernel<false><<<g.ctas, kLifeThreads, smem, s>>>(m, md, src, dst, W, H, pitch, ring, steps, g.T, g.TH, g.LH,
                                                           g.tiles_x, g.tiles_y, err);
   }
   return cudaGetLastError();

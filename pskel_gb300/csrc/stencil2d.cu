@@ -89,7 +89,8 @@ __device__ __forceinline__ void coop_load(TS* dst, const TS* src, int gy0, int g
 
 template <class TS, Op2D OP, bool kTma, int NM>
 __global__ void __launch_bounds__(kStencil2DThreads)
-    stencil2d_kernel(const __grid_constant__ CUtensorMap map_src, const __grid_constant__ CUtensorMap map_u,
+    stencil2d_kernel(const __grid_constant__ CUtensorMap map_src, const __grid_constant__ CUtensorMap map_dst,
+                     const __grid_constant__ CUtensorMap map_u,
                      const __grid_constant__ CUtensorMap map_v, const __grid_constant__ Stencil2DParams p) {
   using S = Storage<TS>;
   using L = Layout<TS, OP>;
@@ -117,6 +118,7 @@ __global__ void __launch_bounds__(kStencil2DThreads)
     mbar_init(bar, 1);
     fence_barrier_init();
     prefetch_tensormap(&map_src);
+    prefetch_tensormap(&map_dst);
     if (OP == Op2D::Advect) {
       prefetch_tensormap(&map_u);
       prefetch_tensormap(&map_v);
@@ -136,12 +138,20 @@ __global__ void __launch_bounds__(kStencil2DThreads)
     const int gy0 = ty * p.TH - p.HY;
     const int gx0 = tx * p.TW - p.HX;
 
+    // Ring cells are never written, so each global buffer keeps its own ring
+    // and the odd steps of a pass read the destination buffer's ring. Tiles
+    // that reach the ring stage the destination tile into bufB for that.
+    const bool touches_ring = (gy0 < p.ring) || (gy0 + LH > p.H - p.ring) || (gx0 < p.ring) ||
+                              (gx0 + LW > p.W - p.ring);
+    const bool stage_dst = touches_ring && p.steps >= 2;
     if (kTma) {
       if (tid == 0) {
         fence_proxy_async();
         const uint32_t tile_bytes = static_cast<uint32_t>(LW * LH * sizeof(TS));
-        mbar_arrive_expect_tx(bar, (OP == Op2D::Advect) ? 3 * tile_bytes : tile_bytes);
+        const uint32_t ntile = 1u + (stage_dst ? 1u : 0u) + (OP == Op2D::Advect ? 2u : 0u);
+        mbar_arrive_expect_tx(bar, ntile * tile_bytes);
         tma_load_2d(bufA, &map_src, gx0, gy0, bar);
+        if (stage_dst) tma_load_2d(bufB, &map_dst, gx0, gy0, bar);
         if (OP == Op2D::Advect) {
           tma_load_2d(bufU, &map_u, gx0, gy0, bar);
           tma_load_2d(bufV, &map_v, gx0, gy0, bar);
@@ -151,6 +161,7 @@ __global__ void __launch_bounds__(kStencil2DThreads)
       phase ^= 1u;
     } else {
       coop_load(bufA, src, gy0, gx0, LW, LH, p.W, p.H, p.pitch);
+      if (stage_dst) coop_load(bufB, static_cast<const TS*>(p.dst), gy0, gx0, LW, LH, p.W, p.H, p.pitch);
       if (OP == Op2D::Advect) {
         coop_load(bufU, static_cast<const TS*>(p.u), gy0, gx0, LW, LH, p.W, p.H, p.pitch);
         coop_load(bufV, static_cast<const TS*>(p.v), gy0, gx0, LW, LH, p.W, p.H, p.pitch);
@@ -178,8 +189,6 @@ __global__ void __launch_bounds__(kStencil2DThreads)
               v = advect_value<TS>(in, bufU, bufV, idx, LW, p);
             }
             out[idx] = S::store(v);
-          } else {
-            out[idx] = in[idx];
           }
         }
       }
@@ -213,32 +222,33 @@ __global__ void __launch_bounds__(kStencil2DThreads)
 }
 
 template <class TS, Op2D OP, bool kTma, int NM>
-cudaError_t launch_one(const CUtensorMap* ms, const CUtensorMap* mu, const CUtensorMap* mv,
+cudaError_t launch_one(const CUtensorMap* ms, const CUtensorMap* md, const CUtensorMap* mu, const CUtensorMap* mv,
                        const Stencil2DParams& p, int ctas, cudaStream_t s) {
   const size_t smem = Layout<TS, OP>::total(p.LW, p.LH);
   auto kern = stencil2d_kernel<TS, OP, kTma, NM>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
-  kern<<<ctas, kStencil2DThreads, smem, s>>>(*ms, *mu, *mv, p);
+  kern<<<ctas, kStencil2DThreads, smem, s>>>(*ms, *md, *mu, *mv, p);
   return cudaGetLastError();
 }
 
 template <class TS, Op2D OP, bool kTma>
-cudaError_t dispatch_nm(const CUtensorMap* ms, const CUtensorMap* mu, const CUtensorMap* mv,
+cudaError_t dispatch_nm(const CUtensorMap* ms, const CUtensorMap* md, const CUtensorMap* mu, const CUtensorMap* mv,
                         const Stencil2DParams& p, int ctas, cudaStream_t s) {
-  if (OP == Op2D::Advect) return launch_one<TS, OP, kTma, 0>(ms, mu, mv, p, ctas, s);
+  if (OP == Op2D::Advect) return launch_one<TS, OP, kTma, 0>(ms, md, mu, mv, p, ctas, s);
   switch (p.nm) {
-    case 4: return launch_one<TS, OP, kTma, 4>(ms, mu, mv, p, ctas, s);
-    case 5: return launch_one<TS, OP, kTma, 5>(ms, mu, mv, p, ctas, s);
-    case 9: return launch_one<TS, OP, kTma, 9>(ms, mu, mv, p, ctas, s);
-    default: return launch_one<TS, OP, kTma, 0>(ms, mu, mv, p, ctas, s);
+    case 4: return launch_one<TS, OP, kTma, 4>(ms, md, mu, mv, p, ctas, s);
+    case 5: return launch_one<TS, OP, kTma, 5>(ms, md, mu, mv, p, ctas, s);
+    case 9: return launch_one<TS, OP, kTma, 9>(ms, md, mu, mv, p, ctas, s);
+    default: return launch_one<TS, OP, kTma, 0>(ms, md, mu, mv, p, ctas, s);
   }
 }
 
 template <class TS, Op2D OP>
-cudaError_t dispatch_tma(bool tma, const CUtensorMap* ms, const CUtensorMap* mu, const CUtensorMap* mv,
+cudaError_t dispatch_tma(bool tma, const CUtensorMap* ms, const CUtensorMap* md, const CUtensorMap* mu,
+                         const CUtensorMap* mv,
                          const Stencil2DParams& p, int ctas, cudaStream_t s) {
-  return tma ? dispatch_nm<TS, OP, true>(ms, mu, mv, p, ctas, s) : dispatch_nm<TS, OP, false>(ms, mu, mv, p, ctas, s);
+  return tma ? dispatch_nm<TS, OP, true>(ms, md, mu, mv, p, ctas, s) : dispatch_nm<TS, OP, false>(ms, md, mu, mv, p, ctas, s);
 }
 
 }  // namespace
@@ -267,15 +277,16 @@ int stencil2d_max_ctas_per_sm(Op2D op, int dtype, int nm, int LW, int LH) {
   return by_smem < by_threads ? by_smem : by_threads;
 }
 
-cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* map_src, const CUtensorMap* map_u,
+cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* map_src, const CUtensorMap* map_dst,
+                           const CUtensorMap* map_u,
                            const CUtensorMap* map_v, const Stencil2DParams& p, int ctas, cudaStream_t s) {
   if (dtype == 2) {
     return op == Op2D::Advect
-               ? dispatch_tma<__nv_bfloat16, Op2D::Advect>(use_tma, map_src, map_u, map_v, p, ctas, s)
-               : dispatch_tma<__nv_bfloat16, Op2D::Linear>(use_tma, map_src, map_u, map_v, p, ctas, s);
+               ? dispatch_tma<__nv_bfloat16, Op2D::Advect>(use_tma, map_src, map_dst, map_u, map_v, p, ctas, s)
+               : dispatch_tma<__nv_bfloat16, Op2D::Linear>(use_tma, map_src, map_dst, map_u, map_v, p, ctas, s);
   }
-  return op == Op2D::Advect ? dispatch_tma<float, Op2D::Advect>(use_tma, map_src, map_u, map_v, p, ctas, s)
-                            : dispatch_tma<float, Op2D::Linear>(use_tma, map_src, map_u, map_v, p, ctas, s);
+  return op == Op2D::Advect ? dispatch_tma<float, Op2D::Advect>(use_tma, map_src, map_dst, map_u, map_v, p, ctas, s)
+                            : dispatch_tma<float, Op2D::Linear>(use_tma, map_src, map_dst, map_u, map_v, p, ctas, s);
 }
 
 }  // namespace pskel

@@ -114,10 +114,11 @@ PSKEL_API const char* pskel_last_error(void);
 /* Wait for `stream`, then report and clear the device error word. */
 PSKEL_API pskel_status pskel_sync(void* stream);
 
-/* Splits `iterations` steps into passes of at most `time_steps` steps, with a
- * pass count of the same parity as `iterations` (so the ping-pong over passes
- * ends in the buffer a step-by-step ping-pong ends in). Writes at most `cap`
- * pass lengths to `passes` and returns the number of passes (host only). */
+/* Splits `iterations` steps into passes of at most `time_steps` steps, each
+ * of an odd length, so that after every pass the state sits in the buffer
+ * (and next to the ring) where a step-by-step ping-pong has it. An even
+ * `time_steps` is lowered by one. Writes at most `cap` pass lengths to
+ * `passes` and returns the number of passes (host only). */
 PSKEL_API int32_t pskel_plan_passes(int64_t iterations, int32_t time_steps, int32_t* passes, int32_t cap);
 
 /* Iterative 2D stencil on device buffers.

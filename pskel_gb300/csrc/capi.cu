@@ -128,22 +128,19 @@ cudaError_t encode_tmap(CUtensorMap* map, CUtensorMapDataType type, int rank, vo
 }
 
 std::vector<int> plan_passes(int64_t iters, int T) {
+  // Every pass has an odd number of steps. Ring cells are never written, so
+  // the reference's state after k steps sits in `out` (k odd) or `in` (k even)
+  // together with that buffer's ring. A pass that reads one buffer and writes
+  // the other therefore has to advance an odd number of steps for the ring it
+  // sees at every step, and the buffer it ends in, to match the reference's.
   std::vector<int> p;
   if (iters <= 0) return p;
-  if (T < 1) T = 1;
-  for (int64_t k = 0; k < iters / T; ++k) p.push_back(T);
-  if (iters % T) p.push_back(static_cast<int>(iters % T));
-  if ((static_cast<int64_t>(p.size()) & 1) != (iters & 1)) {
-    // split the first pass of >= 2 steps in two
-    for (size_t i = 0; i < p.size(); ++i) {
-      if (p[i] >= 2) {
-        const int a = p[i] / 2, b = p[i] - a;
-        p[i] = a;
-        p.insert(p.begin() + static_cast<long>(i) + 1, b);
-        break;
-      }
-    }
-  }
+  const int To = (T <= 1) ? 1 : ((T & 1) ? T : T - 1);
+  int64_t L = (iters + To - 1) / To;
+  if ((L & 1) != (iters & 1)) ++L;  // a sum of L odd numbers has the parity of L
+  const int64_t extra_pairs = (iters - L) / 2;  // each pass: 1 + 2 * (its share of pairs)
+  const int64_t q = extra_pairs / L, r = extra_pairs % L;
+  for (int64_t i = 0; i < L; ++i) p.push_back(static_cast<int>(1 + 2 * (q + (i < r ? 1 : 0))));
   return p;
 }
 
@@ -194,6 +191,7 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
   LifeGeom g;
   int T = (sched && sched->time_steps > 0) ? sched->time_steps : kLifeMaxT;
   T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeMaxT), std::max<int64_t>(iters, 1)));
+  if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
   int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
   TH = std::min(TH, 256 - 2 * T) & ~1;
   if (TH < 2) return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", T);
@@ -240,6 +238,7 @@ static pskel_status iterate_float2d(const pskel_stencil& st, void* in, void* out
   const int vec = static_cast<int>(16 / esz);
   int T = (sched && sched->time_steps > 0) ? sched->time_steps : (op == Op2D::Advect ? 4 : 8);
   T = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(iters, 1)));
+  if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
   if (R == 0) T = 1;  // a mask reaching no neighbour needs no halo
   int TW = (sched && sched->tile_w > 0) ? sched->tile_w : (op == Op2D::Advect ? 64 : 128);
   int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 64;
@@ -250,7 +249,7 @@ static pskel_status iterate_float2d(const pskel_stencil& st, void* in, void* out
     HY = R * T;
     HX = ((R * T + vec - 1) / vec) * vec;
     if ((TW + 2 * HX <= 256 && TH + 2 * HY <= 256) || T == 1) break;
-    --T;
+    T = std::max(1, T - 2);
   }
   if (TW + 2 * HX > 256) TW = std::max(vec, ((256 - 2 * HX) / vec) * vec);
   if (TH + 2 * HY > 256) TH = 256 - 2 * HY;

@@ -96,4 +96,7 @@ def test_pass_plan_parity():
             n = P.lib.pskel_plan_passes(iters, T, buf, 128)
             p = list(buf[:n])
             assert sum(p) == iters and all(1 <= x <= T for x in p)
+            assert all(x % 2 == 1 for x in p)
             assert len(p) % 2 == iters % 2
+            if iters >= T:
+                assert len(p) <= -(-iters // max(1, T - (T + 1) % 2)) + 1

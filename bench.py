@@ -249,9 +249,8 @@ def run_ours(args, wl, world, rank, local):
     st_h = stencil_for(wl, P, S, keep, wind_host)
     esz = pin_in.element_size()
     h2d = W * H * esz * (3 if "u" in x else 1)
-    r = 1
-    if iters % 2 == 1:
-        h2d += (2 * r * W + 2 * r * (H - 2 * r)) * esz
+    r = 1  # the output array's ring goes to the device too (read by every second step)
+    h2d += (2 * r * W + 2 * r * (H - 2 * r)) * esz
     d2h = W * H * esz
 
     def e2e_step():

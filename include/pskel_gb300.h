@@ -135,8 +135,9 @@ PSKEL_API pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* 
 /* Iterative 2D stencil on host arrays: the whole of runIterativeGPU
  * (PSkelStencil.hpp:1046-1097): copy in, iterate, copy the result into
  * `out_host`. `in_host` is not modified; `out_host` must hold the output
- * array's initial contents (its ring is part of the result when iterations
- * is odd). Synchronous. */
+ * array's initial contents: its ring (cells outside r <= h < H-r,
+ * r <= w < W-r) is read by every second step, as in runIterativeCPU, and only
+ * that ring is copied to the device. Synchronous. */
 PSKEL_API pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void* out_host, int64_t width,
                               int64_t height, int64_t iterations, const pskel_schedule* sched);
 

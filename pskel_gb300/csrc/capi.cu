@@ -430,8 +430,9 @@ pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void
   cudaStream_t s = c->stream;
   cudaError_t e = cudaMemcpy2DAsync(c->host_in.ptr, pitch_bytes, in_host, row, row, height, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "copy input to device");
-  if (iterations % 2 == 1 && ring > 0) {
-    // the output array's ring is part of the result when the iteration count is odd
+  if (iterations >= 1 && ring > 0) {
+    // The output array's ring is read by every second step and is part of the
+    // result when the iteration count is odd; its interior is never read.
     const uint8_t* oh = static_cast<const uint8_t*>(out_host);
     uint8_t* od = static_cast<uint8_t*>(c->host_out.ptr);
     const size_t r = static_cast<size_t>(std::min<int64_t>(ring, height));

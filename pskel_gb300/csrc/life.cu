@@ -20,7 +20,16 @@ namespace pskel {
 namespace {
 
 constexpr int kWords = kLifeLW / 32;  // 8 bit words per tile row
-constexpr int kBitPitch = 9;          // padded: 8-row strips land on distinct banks
+// Bit planes hold 256 tile rows plus a zero row above and below, and each row
+// holds a zero word on either side of its 8 words, so the step loop reads
+// neighbours without bounds checks. Pitch 11: the 8-row strips of one warp
+// land on distinct banks.
+constexpr int kBitRows = 256;
+constexpr int kBitPitch = 11;
+constexpr int kBitPlaneWords = (kBitRows + 2) * kBitPitch;
+constexpr int kRowsPerStrip = kBitRows / (kLifeThreads / kWords);  // 8
+
+__device__ __forceinline__ int bit_index(int row, int word) { return (row + 1) * kBitPitch + word + 1; }
 
 // 16 cells (one byte each, value 0/1) -> 16 bits, cell i at bit i.
 __device__ __forceinline__ uint32_t pack16(uint4 v) {
@@ -50,31 +59,48 @@ __device__ __forceinline__ uint32_t bit_range(int lo, int hi) {
   return upto_hi & ~below_lo;
 }
 
-struct RowSums {
-  uint32_t c;       // the row's own cells
-  uint32_t t0, t1;  // west + centre + east, 2-bit sliced
-  uint32_t p0, p1;  // west + east, 2-bit sliced
-};
-
-__device__ __forceinline__ RowSums row_sums(const uint32_t* row, int j) {
-  RowSums r;
-  const uint32_t c = row[j];
-  const uint32_t l = (j > 0) ? row[j - 1] : 0u;
-  const uint32_t e = (j < kWords - 1) ? row[j + 1] : 0u;
-  const uint32_t we = __funnelshift_l(l, c, 1);  // bit b = cell b-1
-  const uint32_t ea = __funnelshift_r(c, e, 1);  // bit b = cell b+1
-  r.c = c;
-  r.t0 = we ^ c ^ ea;
-  r.t1 = (we & c) | (we & ea) | (c & ea);
-  r.p0 = we ^ ea;
-  r.p1 = we & ea;
-  return r;
-}
-
-__device__ __forceinline__ RowSums zero_row() {
-  RowSums r;
-  r.c = r.t0 = r.t1 = r.p0 = r.p1 = 0u;
-  return r;
+// One step for a strip of 8 rows of one word column: the neighbour count of
+// each cell is (w + c + e of the row above) + (w + e of its row) + (w + c + e
+// of the row below), summed with bit-sliced full adders and kept mod 8
+// (a count of 8 aliases to 0, which is dead either way).
+template <bool kMasked>
+__device__ __forceinline__ void life_strip(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int y0, int j,
+                                           uint32_t colmask, int gy0, int ring, int H) {
+  uint32_t c[kRowsPerStrip + 2], t0[kRowsPerStrip + 2], t1[kRowsPerStrip + 2];
+  uint32_t p0[kRowsPerStrip + 2], p1[kRowsPerStrip + 2];
+  const uint32_t* base = in + bit_index(y0 - 1, j);
+#pragma unroll
+  for (int k = 0; k < kRowsPerStrip + 2; ++k) {
+    const uint32_t* r = base + k * kBitPitch;
+    const uint32_t l = r[-1], cc = r[0], e = r[1];
+    const uint32_t we = __funnelshift_l(l, cc, 1);  // bit b = cell b-1
+    const uint32_t ea = __funnelshift_r(cc, e, 1);  // bit b = cell b+1
+    c[k] = cc;
+    t0[k] = we ^ cc ^ ea;
+    t1[k] = (we & cc) | (we & ea) | (cc & ea);
+    p0[k] = we ^ ea;
+    p1[k] = we & ea;
+  }
+  uint32_t* o = out + bit_index(y0, j);
+#pragma unroll
+  for (int k = 1; k <= kRowsPerStrip; ++k) {
+    const uint32_t s0 = t0[k - 1] ^ p0[k] ^ t0[k + 1];
+    const uint32_t k0 = (t0[k - 1] & p0[k]) | (t0[k - 1] & t0[k + 1]) | (p0[k] & t0[k + 1]);
+    const uint32_t x1 = t1[k - 1] ^ p1[k] ^ t1[k + 1];
+    const uint32_t y1 = (t1[k - 1] & p1[k]) | (t1[k - 1] & t1[k + 1]) | (p1[k] & t1[k + 1]);
+    const uint32_t s1 = x1 ^ k0;
+    const uint32_t s2 = y1 ^ (x1 & k0);
+    const uint32_t alive = s1 & ~s2 & (s0 | c[k]);  // count 3, or count 2 and alive
+    uint32_t* dst = o + (k - 1) * kBitPitch;
+    if (kMasked) {
+      // cells outside r <= h < H-r, r <= w < W-r keep the value this plane holds
+      const int gy = gy0 + y0 + k - 1;
+      const uint32_t m = (gy >= ring && gy < H - ring) ? colmask : 0u;
+      *dst = (alive & m) | (*dst & ~m);
+    } else {
+      *dst = alive;
+    }
+  }
 }
 
 template <bool kTma>
@@ -86,10 +112,13 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* bytes = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   uint32_t* bitsA = reinterpret_cast<uint32_t*>(bytes + LH * kLifeLW);
-  uint32_t* bitsB = bitsA + LH * kBitPitch;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(bitsB + LH * kBitPitch + ((LH * kBitPitch) & 1));
+  uint32_t* bitsB = bitsA + kBitPlaneWords;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(bitsB + kBitPlaneWords);
 
   const int tid = threadIdx.x;
+  // zero both planes once: the padding rows/words are never written again and
+  // rows at or beyond LH stay zero until the first tile's steps run over them
+  for (int i = tid; i < 2 * kBitPlaneWords; i += kLifeThreads) bitsA[i] = 0u;
   if (kTma && tid == 0) {
     mbar_init(bar, 1);
     fence_barrier_init();
@@ -102,10 +131,18 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
   bool bad_value = false;
   const int ntiles = tiles_x * tiles_y;
   const int j = tid & (kWords - 1);
-  const int strip = tid >> 3;                 // 32 strips of rows
-  const int rps = (LH + 31) >> 5;             // rows per strip
-  const int ya = strip * rps;
-  const int yb = min(LH, ya + rps);
+  const int y0 = (tid >> 3) * kRowsPerStrip;  // 32 strips of 8 rows
+
+  // The byte tile is free again as soon as it is packed into bits, so the
+  // next tile's TMA load is issued before this tile's steps run.
+  auto issue_load = [&](int t, const CUtensorMap* m) {
+    const int ty = t / tiles_x;
+    const int tx = t - ty * tiles_x;
+    fence_proxy_async();
+    mbar_arrive_expect_tx(bar, static_cast<uint32_t>(LH * kLifeLW));
+    tma_load_2d(bytes, m, tx * kLifeTW - kLifeHX, ty * TH - T, bar);
+  };
+  if (kTma && tid == 0 && static_cast<int>(blockIdx.x) < ntiles) issue_load(blockIdx.x, &map);
 
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int ty = tile / tiles_x;
@@ -120,13 +157,11 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
     const bool touches_ring = (gy0 < ring) || (gy0 + LH > H - ring) || (gx0 < ring) || (gx0 + kLifeLW > W - ring);
     const int nstage = (touches_ring && steps >= 2) ? 2 : 1;
     for (int k = 0; k < nstage; ++k) {
-      if (k == 1) __syncthreads();  // the byte tile is reused
+      if (k == 1) {
+        __syncthreads();  // the byte tile is reused
+        if (kTma && tid == 0) issue_load(tile, &map_dst);
+      }
       if (kTma) {
-        if (tid == 0) {
-          fence_proxy_async();
-          mbar_arrive_expect_tx(bar, static_cast<uint32_t>(LH * kLifeLW));
-          tma_load_2d(bytes, k == 0 ? &map : &map_dst, gx0, gy0, bar);
-        }
         if (!mbar_wait_bounded(bar, phase, err)) return;
         phase ^= 1u;
       } else {
@@ -178,36 +213,25 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
         }
         const uint32_t half = pack16(v);
         const uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, half, 1);
-        if ((c & 1) == 0) plane[row * kBitPitch + (c >> 1)] = half | (other << 16);
+        if ((c & 1) == 0) plane[bit_index(row, c >> 1)] = half | (other << 16);
       }
+      // rows [LH, 256) of the plane restart from zero for every tile
+      for (int i = LH * kWords + tid; i < kBitRows * kWords; i += kLifeThreads)
+        plane[bit_index(i >> 3, i & 7)] = 0u;
     }
     __syncthreads();
+    if (kTma && tid == 0 && tile + static_cast<int>(gridDim.x) < ntiles) issue_load(tile + gridDim.x, &map);
 
-    // ---- the steps, on bit planes
+    // ---- the steps, on bit planes. Rows at or beyond LH are computed too
+    // (from zeros); like the tile edges they only feed the halo.
     const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
     for (int s = 0; s < steps; ++s) {
       const uint32_t* in = (s & 1) ? bitsB : bitsA;
       uint32_t* out = (s & 1) ? bitsA : bitsB;
-      if (ya < yb) {
-        RowSums prev = (ya > 0) ? row_sums(in + (ya - 1) * kBitPitch, j) : zero_row();
-        RowSums cur = row_sums(in + ya * kBitPitch, j);
-        for (int y = ya; y < yb; ++y) {
-          const RowSums next = (y + 1 < LH) ? row_sums(in + (y + 1) * kBitPitch, j) : zero_row();
-          // neighbour count = prev(w,c,e) + cur(w,e) + next(w,c,e), kept mod 8
-          const uint32_t s0 = prev.t0 ^ cur.p0 ^ next.t0;
-          const uint32_t k0 = (prev.t0 & cur.p0) | (prev.t0 & next.t0) | (cur.p0 & next.t0);
-          const uint32_t x1 = prev.t1 ^ cur.p1 ^ next.t1;
-          const uint32_t y1 = (prev.t1 & cur.p1) | (prev.t1 & next.t1) | (cur.p1 & next.t1);
-          const uint32_t s1 = x1 ^ k0;
-          const uint32_t s2 = y1 ^ (x1 & k0);
-          const uint32_t alive = s1 & ~s2 & (s0 | cur.c);  // count 3, or count 2 and alive
-          const int gy = gy0 + y;
-          const uint32_t m = (gy >= ring && gy < H - ring) ? colmask : 0u;
-          uint32_t* o = out + y * kBitPitch + j;
-          *o = (m == 0xFFFFFFFFu) ? alive : ((alive & m) | (*o & ~m));
-          prev = cur;
-          cur = next;
-        }
+      if (touches_ring) {
+        life_strip<true>(in, out, y0, j, colmask, gy0, ring, H);
+      } else {
+        life_strip<false>(in, out, y0, j, colmask, gy0, ring, H);
       }
       __syncthreads();
     }
@@ -222,7 +246,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
       if (gy < ring || gy >= H - ring) continue;
       const int gx = gx0 + c * 16;
       if (gx + 16 <= ring || gx >= W - ring) continue;
-      const uint32_t word = fin[row * kBitPitch + (c >> 1)];
+      const uint32_t word = fin[bit_index(row, c >> 1)];
       const uint4 v = unpack16((c & 1) ? (word >> 16) : (word & 0xFFFFu));
       uint8_t* d = dst + static_cast<int64_t>(gy) * pitch + gx;
       if (gx >= ring && gx + 16 <= W - ring && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
@@ -244,7 +268,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
 }  // namespace
 
 size_t life_smem_bytes(int LH) {
-  return 128 + static_cast<size_t>(LH) * kLifeLW + 2 * static_cast<size_t>(LH) * kBitPitch * 4 + 16;
+  return 128 + static_cast<size_t>(LH) * kLifeLW + 2 * static_cast<size_t>(kBitPlaneWords) * 4 + 16;
 }
 
 int life_max_ctas_per_sm(int LH) {

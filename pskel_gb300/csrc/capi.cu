@@ -189,21 +189,49 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
                                  int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,
                                  cudaStream_t s) {
   LifeGeom g;
-  int T = (sched && sched->time_steps > 0) ? sched->time_steps : kLifeMaxT;
-  T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeMaxT), std::max<int64_t>(iters, 1)));
-  if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
-  int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
-  TH = std::min(TH, 256 - 2 * T) & ~1;
-  if (TH < 2) return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", T);
-  g.T = T;
-  g.TH = TH;
-  g.LH = TH + 2 * T;
-  g.tiles_x = static_cast<int>((W + kLifeTW - 1) / kLifeTW);
-  g.tiles_y = static_cast<int>((H + TH - 1) / TH);
-  const int ntiles = g.tiles_x * g.tiles_y;
-  const int per_sm = life_max_ctas_per_sm(g.LH);
-  g.ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
-  g.ctas = std::max(1, std::min(g.ctas, ntiles));
+  const int per_sm = life_max_ctas_per_sm(256);
+  const int64_t it1 = std::max<int64_t>(iters, 1);
+  auto geom_for = [&](int T, LifeGeom& out) -> bool {
+    T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeMaxT), it1));
+    if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
+    int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
+    TH = std::min(TH, 256 - 2 * T) & ~1;
+    if (TH < 2) return false;
+    out.T = T;
+    out.TH = TH;
+    out.LH = TH + 2 * T;
+    out.tiles_x = static_cast<int>((W + kLifeTW - 1) / kLifeTW);
+    out.tiles_y = static_cast<int>((H + TH - 1) / TH);
+    const int ntiles = out.tiles_x * out.tiles_y;
+    out.ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
+    out.ctas = std::max(1, std::min(out.ctas, ntiles));
+    return true;
+  };
+  if (sched && sched->time_steps > 0) {
+    if (!geom_for(sched->time_steps, g))
+      return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", sched->time_steps);
+  } else {
+    // Default schedule: every tile costs about the same (the bit planes are
+    // always 256 rows), so the run costs (passes) x (waves of tiles over the
+    // resident CTAs). Pick the odd temporal block minimising that product.
+    double best = 0;
+    bool found = false;
+    for (int T = kLifeMaxT - 1; T >= 5; T -= 2) {
+      LifeGeom cand;
+      if (!geom_for(T, cand)) continue;
+      const int64_t passes = static_cast<int64_t>(plan_passes(iters, cand.T).size());
+      const int64_t slots = static_cast<int64_t>(per_sm) * c->sms;
+      const int64_t waves = (static_cast<int64_t>(cand.tiles_x) * cand.tiles_y + slots - 1) / slots;
+      const double cost = static_cast<double>(passes) * static_cast<double>(waves);
+      if (!found || cost < best) {
+        best = cost;
+        g = cand;
+        found = true;
+      }
+      if (cand.T < T) break;  // iterations cap the block: smaller T only adds passes
+    }
+    if (!found && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
+  }
   const bool use_tma = tma_ok(in, pitch) && tma_ok(out, pitch);
   CUtensorMap map_in, map_out;
   memset(&map_in, 0, sizeof(map_in));
@@ -211,12 +239,12 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
   if (use_tma) {
     const uint64_t dims[2] = {static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
     const uint64_t strides[1] = {static_cast<uint64_t>(pitch)};
-    const uint32_t box[2] = {static_cast<uint32_t>(kLifeLW), static_cast<uint32_t>(g.LH)};
+    const uint32_t box[2] = {static_cast<uint32_t>(kLifeLW), 64u};  // one 64-row chunk per load
     cudaError_t e = encode_tmap(&map_in, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, in, dims, strides, box);
     if (e == cudaSuccess) e = encode_tmap(&map_out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, out, dims, strides, box);
     if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled");
   }
-  const std::vector<int> passes = plan_passes(iters, T);
+  const std::vector<int> passes = plan_passes(iters, g.T);
   for (size_t i = 0; i < passes.size(); ++i) {
     const bool fwd = (i % 2 == 0);
     const uint8_t* src = static_cast<const uint8_t*>(fwd ? in : out);

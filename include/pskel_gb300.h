@@ -141,6 +141,28 @@ PSKEL_API pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* 
 PSKEL_API pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void* out_host, int64_t width,
                               int64_t height, int64_t iterations, const pskel_schedule* sched);
 
+/* Iterative 3D stencil on device buffers (linear mask, f32 or bf16).
+ * Replaces Stencil3D::runIterativeGPU / runIterativeTilingGPU
+ * (PSkelStencil.h:258, 292; PSkelStencil.hpp:1046-1097, 1663-1862), whose 3D
+ * instantiation the reference cannot compile, with the semantics of
+ * Stencil3D::runIterativeCPU (PSkelStencil.hpp:880-938, 2104-2113): every cell
+ * is written each step, out-of-grid neighbours read mask.halo_value.
+ * schedule.time_steps steps are fused per pass (2.5D streaming along h).
+ * When residual_every > 0, residuals[k/residual_every - 1] receives the fp64
+ * norm ||u_k - u_{k-1}||_2 for every k that is a multiple of residual_every
+ * (device array of iterations/residual_every doubles). */
+PSKEL_API pskel_status pskel_iterate3d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height,
+                                       int64_t depth, int64_t iterations, const pskel_schedule* sched,
+                                       int64_t residual_every, double* residuals, void* stream);
+
+/* Iterative 3D stencil on host arrays (copy in, iterate, copy the result into
+ * out_host, residual norms into residuals_host). `in_host` is not modified;
+ * the output array's initial contents are never read. Synchronous. */
+PSKEL_API pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_host, void* out_host, int64_t width,
+                                        int64_t height, int64_t depth, int64_t iterations,
+                                        const pskel_schedule* sched, int64_t residual_every,
+                                        double* residuals_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,10 @@ def _load():
     lib.pskel_plan_passes.restype = C.c_int32
     lib.pskel_run2d_host.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                      C.POINTER(Schedule)]
+    lib.pskel_iterate3d.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                    C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p, C.c_void_p]
+    lib.pskel_run3d_host.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                     C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p]
     return lib
 
 
@@ -142,3 +146,24 @@ def run2d_host(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int
     _check(lib.pskel_run2d_host(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, iterations,
                                 C.byref(sc) if sc is not None else None))
     return a_out
+
+
+def iterate3d(st: Stencil, a_in, a_out, iterations: int, sched=None, residual_every: int = 0, residuals=None,
+              stream=None):
+    """Device-buffer 3D run; arrays are [H][W][D] (d fastest). Asynchronous."""
+    H, W, D = a_in.shape
+    sc = make_schedule(sched)
+    _check(lib.pskel_iterate3d(C.byref(st), _ptr(a_in), _ptr(a_out), W, H, D, iterations,
+                               C.byref(sc) if sc is not None else None, residual_every, _ptr(residuals), stream))
+
+
+def run3d_host(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int, sched=None, residual_every=0):
+    """Stencil3D::runIterativeGPU on host arrays; returns (output, residual norms)."""
+    assert a_in.flags.c_contiguous and a_out.flags.c_contiguous
+    H, W, D = a_in.shape
+    n = iterations // residual_every if residual_every > 0 else 0
+    res = np.zeros(max(n, 1), dtype=np.float64)
+    sc = make_schedule(sched)
+    _check(lib.pskel_run3d_host(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, D, iterations,
+                                C.byref(sc) if sc is not None else None, residual_every, res.ctypes.data))
+    return a_out, res[:n]

@@ -144,6 +144,28 @@ std::vector<int> plan_passes(int64_t iters, int T) {
   return p;
 }
 
+std::vector<int> plan_passes_any(int64_t iters, int T) {
+  // Passes of at most T steps (any length) whose count has the parity of
+  // `iters`, so a ping-pong over the passes ends in the buffer a step-by-step
+  // ping-pong ends in. For grids where every cell is written each step.
+  std::vector<int> p;
+  if (iters <= 0) return p;
+  if (T < 1) T = 1;
+  for (int64_t k = 0; k < iters / T; ++k) p.push_back(T);
+  if (iters % T) p.push_back(static_cast<int>(iters % T));
+  if ((static_cast<int64_t>(p.size()) & 1) != (iters & 1)) {
+    for (size_t i = 0; i < p.size(); ++i) {
+      if (p[i] >= 2) {
+        const int a = p[i] / 2, b = p[i] - a;
+        p[i] = a;
+        p.insert(p.begin() + static_cast<long>(i) + 1, b);
+        break;
+      }
+    }
+  }
+  return p;
+}
+
 // --------------------------------------------------------------- validation
 
 static size_t dtype_size(pskel_dtype d) { return d == PSKEL_U8 ? 1 : (d == PSKEL_F32 ? 4 : 2); }
@@ -401,6 +423,125 @@ pskel_status validate2d(const pskel_stencil* st, const void* in, const void* out
   return PSKEL_OK;
 }
 
+// ------------------------------------------------------------- 3D iterate
+
+pskel_status validate3d(const pskel_stencil* st, const void* in, const void* out, int64_t W, int64_t H, int64_t D,
+                        int64_t iters, int64_t every, int* R) {
+  if (!st) return fail(PSKEL_ERR_INVALID, "stencil descriptor is NULL");
+  if (!in || !out) return fail(PSKEL_ERR_INVALID, "grid buffer pointer is NULL");
+  if (in == out) return fail(PSKEL_ERR_INVALID, "input and output must be distinct buffers");
+  if (W <= 0 || H <= 0 || D <= 0) return fail(PSKEL_ERR_INVALID, "3D grid is empty");
+  if (W >= (int64_t(1) << 31) || H >= (int64_t(1) << 31) || D >= (int64_t(1) << 31))
+    return fail(PSKEL_ERR_UNSUPPORTED, "grid side >= 2^31");
+  if (iters < 0) return fail(PSKEL_ERR_INVALID, "negative iteration count");
+  if (every < 0) return fail(PSKEL_ERR_INVALID, "negative residual interval");
+  if (st->op != PSKEL_OP_LINEAR) return fail(PSKEL_ERR_UNSUPPORTED, "3D grids support the linear mask stencil");
+  if (st->dtype != PSKEL_F32 && st->dtype != PSKEL_BF16)
+    return fail(PSKEL_ERR_UNSUPPORTED, "3D stencil supports f32 and bf16 storage");
+  if (st->mask.size > kMaxMask3D) return fail(PSKEL_ERR_UNSUPPORTED, "3D mask larger than %d entries", kMaxMask3D);
+  int ring = 0;
+  if (pskel_status s = check_mask(st->mask, 3, true, R, &ring)) return s;
+  if (*R > 3) return fail(PSKEL_ERR_UNSUPPORTED, "3D mask reach %d > 3", *R);
+  return PSKEL_OK;
+}
+
+static pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
+                              int64_t iters, int R, const pskel_schedule* sched, int64_t every, double* residuals,
+                              double* partials_override, int64_t partials_cap, DeviceContext* c, cudaStream_t s) {
+  const int dtype = static_cast<int>(st.dtype);
+  const size_t esz = dtype_size(st.dtype);
+  const int vec = static_cast<int>(16 / esz);
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : 2;
+  T = static_cast<int>(std::min<int64_t>(std::min(T, kMax3DSteps), std::max<int64_t>(iters, 1)));
+  if (R == 0) T = 1;
+  int TW = (sched && sched->tile_w > 0) ? sched->tile_w : 32;
+  int TD = (sched && sched->tile_d > 0) ? sched->tile_d : 64;
+  TD = std::max(vec, (TD / vec) * vec);
+  Stencil3DParams p;
+  memset(&p, 0, sizeof(p));
+  int LW = 0, LD = 0, HW = 0, HD = 0;
+  size_t smem = 0;
+  for (;;) {
+    HW = R * T;
+    HD = ((R * T + vec - 1) / vec) * vec;
+    LW = TW + 2 * HW;
+    LD = TD + 2 * HD;
+    smem = stencil3d_smem_bytes(LW, LD, 2 * R + 1, T, esz);
+    if ((smem <= static_cast<size_t>(c->smem_optin) && LD <= 256 && LW <= 256) || (T == 1 && TW <= 8)) break;
+    if (T > 1) --T; else TW = std::max(1, TW / 2);
+  }
+  if (smem > static_cast<size_t>(c->smem_optin) || LD > 256 || LW > 256)
+    return fail(PSKEL_ERR_UNSUPPORTED, "3D tile does not fit in shared memory");
+  p.W = static_cast<int>(W);
+  p.H = static_cast<int>(H);
+  p.D = static_cast<int>(D);
+  p.R = R;
+  p.NP = 2 * R + 1;
+  p.T = T;
+  p.TW = TW;
+  p.TD = TD;
+  p.LW = LW;
+  p.LD = LD;
+  p.HW = HW;
+  p.HD = HD;
+  p.tiles_w = static_cast<int>((W + TW - 1) / TW);
+  p.tiles_d = static_cast<int>((D + TD - 1) / TD);
+  p.nm = st.mask.size;
+  for (int n = 0; n < p.nm; ++n) {
+    p.off_h[n] = st.mask.offsets[3 * n];
+    p.off_plane[n] = st.mask.offsets[3 * n + 1] * LD + st.mask.offsets[3 * n + 2];
+    p.wt[n] = st.mask.weights[n];
+  }
+  p.halo = st.mask.halo_value;
+  p.err = c->err;
+  p.every = static_cast<int>(every);
+  p.residuals = residuals;
+  const int ntiles = p.tiles_w * p.tiles_d;
+  const int per_sm = std::max(1, stencil3d_max_ctas_per_sm(smem));
+  int ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
+  ctas = std::max(1, std::min(ctas, ntiles));
+  if (every > 0) {
+    const size_t need = static_cast<size_t>(T) * ctas;
+    if (partials_override) {
+      if (static_cast<int64_t>(need) > partials_cap)
+        return fail(PSKEL_ERR_UNSUPPORTED, "residual scratch of %zu partials exceeds the fixed capacity %lld", need,
+                    (long long)partials_cap);
+      p.partials = partials_override;
+    } else {
+      if (pskel_status q = ensure_buffer(c->partials, need * sizeof(double))) return q;
+      p.partials = static_cast<double*>(c->partials.ptr);
+    }
+  }
+  const int64_t Db = D * static_cast<int64_t>(esz);
+  const bool use_tma = (reinterpret_cast<uintptr_t>(in) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
+                       (Db & 15) == 0;
+  CUtensorMap m_in, m_out;
+  memset(&m_in, 0, sizeof(m_in));
+  memset(&m_out, 0, sizeof(m_out));
+  if (use_tma) {
+    const CUtensorMapDataType tt = (dtype == PSKEL_BF16) ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const uint64_t dims[3] = {static_cast<uint64_t>(D), static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
+    const uint64_t strides[2] = {static_cast<uint64_t>(Db), static_cast<uint64_t>(Db * W)};
+    const uint32_t box[3] = {static_cast<uint32_t>(LD), static_cast<uint32_t>(LW), 1u};
+    cudaError_t e = encode_tmap(&m_in, tt, 3, in, dims, strides, box);
+    if (e == cudaSuccess) e = encode_tmap(&m_out, tt, 3, out, dims, strides, box);
+    if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled (3D)");
+  }
+  const std::vector<int> passes = plan_passes_any(iters, T);
+  int64_t done = 0;
+  for (size_t i = 0; i < passes.size(); ++i) {
+    const bool fwd = (i % 2 == 0);
+    p.src = fwd ? in : out;
+    p.dst = fwd ? out : in;
+    p.steps = passes[i];
+    p.step0 = done;
+    cudaError_t e = stencil3d_pass(dtype, use_tma, fwd ? &m_in : &m_out, p, ctas, s);
+    if (e != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
+    done += passes[i];
+  }
+  return PSKEL_OK;
+}
+
 }  // namespace pskel
 
 using namespace pskel;
@@ -496,6 +637,53 @@ pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void
     return q;
   const void* result = (iterations % 2 == 1) ? c->host_out.ptr : c->host_in.ptr;
   e = cudaMemcpy2DAsync(out_host, row, result, pitch_bytes, row, height, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy result to host");
+  return device_sync_check(c, s);
+}
+
+pskel_status pskel_iterate3d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height, int64_t depth,
+                             int64_t iterations, const pskel_schedule* sched, int64_t residual_every,
+                             double* residuals, void* stream) {
+  clear_error();
+  int R = 0;
+  if (pskel_status s = validate3d(st, in, out, width, height, depth, iterations, residual_every, &R)) return s;
+  if (residual_every > 0 && iterations >= residual_every && !residuals)
+    return fail(PSKEL_ERR_INVALID, "residual output pointer is NULL");
+  if (iterations == 0) return PSKEL_OK;
+  DeviceContext* c = nullptr;
+  if (pskel_status s = get_context(&c)) return s;
+  return iterate3d(*st, in, out, width, height, depth, iterations, R, sched, residual_every, residuals, nullptr, 0, c,
+                   static_cast<cudaStream_t>(stream));
+}
+
+pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_host, void* out_host, int64_t width,
+                              int64_t height, int64_t depth, int64_t iterations, const pskel_schedule* sched,
+                              int64_t residual_every, double* residuals_host) {
+  clear_error();
+  int R = 0;
+  if (!in_host || !out_host) return fail(PSKEL_ERR_INVALID, "host array pointer is NULL");
+  if (pskel_status s = validate3d(st, in_host, out_host, width, height, depth, iterations, residual_every, &R)) return s;
+  const int64_t nres = residual_every > 0 ? iterations / residual_every : 0;
+  if (nres > 0 && !residuals_host) return fail(PSKEL_ERR_INVALID, "residual output pointer is NULL");
+  DeviceContext* c = nullptr;
+  if (pskel_status s = get_context(&c)) return s;
+  const size_t bytes = static_cast<size_t>(width) * height * depth * dtype_size(st->dtype);
+  if (pskel_status s = ensure_buffer(c->host_in, bytes)) return s;
+  if (pskel_status s = ensure_buffer(c->host_out, bytes)) return s;
+  if (nres > 0)
+    if (pskel_status s = ensure_buffer(c->residuals, static_cast<size_t>(nres) * sizeof(double))) return s;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaMemcpyAsync(c->host_in.ptr, in_host, bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy input to device");
+  if (pskel_status q = iterate3d(*st, c->host_in.ptr, c->host_out.ptr, width, height, depth, iterations, R, sched,
+                                 residual_every, static_cast<double*>(c->residuals.ptr), nullptr, 0, c, s))
+    return q;
+  // every cell is written each step, so the result is whole in one buffer
+  const void* result = (iterations % 2 == 1) ? c->host_out.ptr : c->host_in.ptr;
+  e = cudaMemcpyAsync(out_host, result, bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && nres > 0)
+    e = cudaMemcpyAsync(residuals_host, c->residuals.ptr, static_cast<size_t>(nres) * sizeof(double),
+                        cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "copy result to host");
   return device_sync_check(c, s);
 }

@@ -21,6 +21,8 @@ struct DeviceContext {
   unsigned* err = nullptr;        // device error word (kernels atomicOr into it)
   cudaStream_t stream = nullptr;  // stream of the *_host entry points
   DeviceBuffer host_in, host_out, host_u, host_v;  // staging for *_host
+  DeviceBuffer partials;                           // 3D residual: per-CTA fp64 partial sums
+  DeviceBuffer residuals;                          // 3D residual norms for *_host
 };
 
 pskel_status fail(pskel_status code, const char* fmt, ...);

@@ -81,4 +81,38 @@ cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* 
                            const CUtensorMap* map_u,
                            const CUtensorMap* map_v, const Stencil2DParams& p, int ctas, cudaStream_t s);
 
+// ------------------------------------------------------- 3D float stencils
+
+constexpr int kMaxMask3D = 32;
+constexpr int kMax3DSteps = 8;  // time steps fused per pass
+constexpr int kStencil3DThreads = 256;
+
+struct Stencil3DParams {
+  int W, H, D;        // h slowest, d fastest
+  int R;              // max |offset|
+  int NP;             // planes per level ring = 2R + 1
+  int steps, T;       // steps in this pass, geometry steps
+  int TW, TD;         // core tile in (w, d)
+  int LW, LD;         // plane window
+  int HW, HD;         // halos in w and d
+  int tiles_w, tiles_d;
+  int nm;
+  int off_h[kMaxMask3D];      // dh per entry
+  int off_plane[kMaxMask3D];  // dw * LD + dd per entry
+  float wt[kMaxMask3D];
+  float halo;
+  const void* src;
+  void* dst;
+  unsigned* err;
+  int64_t step0;       // steps completed before this pass
+  int every;           // report ||u_g - u_{g-1}|| when g % every == 0 (0: never)
+  double* partials;    // scratch: steps x ctas fp64 partial sums
+  double* residuals;   // device: one norm per reported step
+};
+
+size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize);
+int stencil3d_max_ctas_per_sm(size_t smem);
+cudaError_t stencil3d_pass(int dtype, bool use_tma, const CUtensorMap* map_src, const Stencil3DParams& p, int ctas,
+                           cudaStream_t s);
+
 }  // namespace pskel

@@ -1,0 +1,277 @@
+// 3D weighted-mask stencils (fp32 / bf16 storage), 2.5D streaming with
+// temporal blocking, and the fused fp64 residual norm.
+//
+// Layout is the reference's (PSkelArray.hpp:349-352): element (h, w, d) at
+// [(h * W + w) * D + d], d fastest. Every cell is updated; a neighbour outside
+// the grid reads the mask's halo value (Mask3D::get, PSkelMask.hpp:186-199;
+// Stencil3D::runOpenMP visits every cell, PSkelStencil.hpp:2104-2113).
+//
+// Each persistent CTA owns a (w, d) tile column and marches along h. For a
+// pass of `steps` time steps it keeps, per time level k < steps, a ring of
+// 2R+1 planes of the tile window in shared memory. At march position i, level
+// 0 receives input plane i (one 3D TMA load of a one-plane box, prefetched a
+// plane ahead), and level k computes plane i - k*R from level k-1's planes
+// i - k*R - R .. i - k*R + R. Level `steps` goes straight to global memory.
+// The (w, d) region computed at level k shrinks by R per level: the halo of
+// R*T cells is recomputed redundantly by neighbouring tiles.
+//
+// Residual: when global step g (1-based) is a multiple of `every`, the CTA
+// accumulates sum((u_g - u_{g-1})^2) over its core cells in fp64 and writes
+// one partial per (reported step, CTA) to a scratch array; reduce3d_residual
+// then adds the partials of each reported step in a fixed order, so the norm
+// does not depend on thread timing.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pskel {
+namespace {
+
+template <class TS>
+__host__ __device__ inline size_t plane_bytes(int LW, int LD) {
+  return (static_cast<size_t>(LW) * LD * sizeof(TS) + 127) & ~size_t(127);
+}
+
+template <class TS>
+__device__ __forceinline__ void fill_plane(TS* pl, int n, TS v) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) pl[i] = v;
+}
+
+template <class TS, int NM, bool kTma>
+__global__ void __launch_bounds__(kStencil3DThreads)
+    stencil3d_kernel(const __grid_constant__ CUtensorMap map_src, const __grid_constant__ Stencil3DParams p) {
+  using S = Storage<TS>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  const int LW = p.LW, LD = p.LD, NP = p.NP, R = p.R;
+  const int plane_elems = LW * LD;
+  const size_t pb = plane_bytes<TS>(LW, LD);
+  // level 0 ring has one extra slot so the next plane can load while the
+  // current ones are still read; levels 1..steps-1 have NP slots each
+  const int NP0 = NP + 1;
+  TS* lvl0 = reinterpret_cast<TS*>(base);
+  auto level_plane = [&](int k, int q) -> TS* {
+    if (k == 0) return reinterpret_cast<TS*>(base + static_cast<size_t>((q % NP0 + NP0) % NP0) * pb);
+    return reinterpret_cast<TS*>(base + (NP0 + static_cast<size_t>(k - 1) * NP + (q % NP + NP) % NP) * pb);
+  };
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + (NP0 + static_cast<size_t>(p.T - 1) * NP) * pb);
+
+  __shared__ int s_offh[kMaxMask3D], s_offp[kMaxMask3D];
+  __shared__ float s_wt[kMaxMask3D];
+  // fp64 residual partials per (level of this pass, warp); each warp adds
+  // its own reduced sums in march order, so the partials are deterministic
+  __shared__ double s_part[kMax3DSteps][kStencil3DThreads / 32];
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  constexpr int kWarps = kStencil3DThreads / 32;
+  for (int i = tid; i < kMax3DSteps * (kStencil3DThreads / 32); i += kStencil3DThreads) (&s_part[0][0])[i] = 0.0;
+  if (tid < p.nm) {
+    s_offh[tid] = p.off_h[tid];
+    s_offp[tid] = p.off_plane[tid];
+    s_wt[tid] = p.wt[tid];
+  }
+  if (kTma && tid == 0) {
+    mbar_init(bar, 1);
+    fence_barrier_init();
+    prefetch_tensormap(&map_src);
+  }
+  __syncthreads();
+  (void)lvl0;
+
+  const TS halo = S::store(p.halo);
+  const TS* src = static_cast<const TS*>(p.src);
+  TS* dst = static_cast<TS*>(p.dst);
+  const int ntiles = p.tiles_w * p.tiles_d;
+  const int steps = p.steps;
+  uint32_t phase = 0;
+
+  const int last = p.H - 1 + steps * R;  // march positions 0..last
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int tw = tile / p.tiles_d;
+    const int td = tile - tw * p.tiles_d;
+    const int gw0 = tw * p.TW - p.HW;  // global w of local w 0
+    const int gd0 = td * p.TD - p.HD;  // global d of local d 0
+    const bool edge = (gw0 < 0) || (gw0 + LW > p.W) || (gd0 < 0) || (gd0 + LD > p.D);
+
+    // planes before the grid read the halo value at every level
+    for (int k = 0; k < steps; ++k)
+      for (int q = -R; q < 0; ++q) fill_plane(level_plane(k, q), plane_elems, halo);
+    __syncthreads();
+
+    auto issue = [&](int plane) {
+      fence_proxy_async();
+      mbar_arrive_expect_tx(bar, static_cast<uint32_t>(plane_elems * sizeof(TS)));
+      tma_load_3d(level_plane(0, plane), &map_src, gd0, gw0, plane, bar);
+    };
+    if (kTma && tid == 0 && p.H > 0) issue(0);
+
+    for (int i = 0; i <= last; ++i) {
+      // ---- level 0: input plane i
+      if (i < p.H && !kTma) {
+        TS* pl = level_plane(0, i);
+        for (int e = tid; e < plane_elems; e += kStencil3DThreads) {
+          const int lw = e / LD, ld = e - lw * LD;
+          const int gw = gw0 + lw, gd = gd0 + ld;
+          pl[e] = (gw < 0 || gw >= p.W || gd < 0 || gd >= p.D) ? halo
+                                                                : src[(static_cast<int64_t>(i) * p.W + gw) * p.D + gd];
+        }
+      } else if (i < p.H) {
+        if (!mbar_wait_bounded(bar, phase, p.err)) return;
+        phase ^= 1u;
+        if (edge && S::load(halo) != 0.0f) {
+          TS* pl = level_plane(0, i);
+          for (int e = tid; e < plane_elems; e += kStencil3DThreads) {
+            const int lw = e / LD, ld = e - lw * LD;
+            const int gw = gw0 + lw, gd = gd0 + ld;
+            if (gw < 0 || gw >= p.W || gd < 0 || gd >= p.D) pl[e] = halo;
+          }
+        }
+      } else {
+        fill_plane(level_plane(0, i), plane_elems, halo);
+      }
+      __syncthreads();
+      // the slot of plane i+1 held plane i-NP-... no longer read: prefetch it
+      if (kTma && tid == 0 && i + 1 < p.H) issue(i + 1);
+
+      // ---- levels 1..steps
+      for (int k = 1; k <= steps; ++k) {
+        const int q = i - k * R;
+        if (q < 0) continue;
+        if (k < steps && q >= p.H) {
+          fill_plane(level_plane(k, q), plane_elems, halo);
+          __syncthreads();
+          continue;
+        }
+        if (q >= p.H) continue;
+        const int e = R * (steps - k);
+        const int w_lo = p.HW - e, w_hi = p.HW + p.TW + e;
+        const int d_lo = p.HD - e, d_hi = p.HD + p.TD + e;
+        const TS* nb[NM > 0 ? NM : kMaxMask3D];
+        const int nm = NM > 0 ? NM : p.nm;
+#pragma unroll
+        for (int n = 0; n < (NM > 0 ? NM : kMaxMask3D); ++n)
+          if (n < nm) nb[n] = level_plane(k - 1, q + s_offh[n]) + s_offp[n];
+        TS* outp = (k < steps) ? level_plane(k, q) : nullptr;
+        const TS* prevp = level_plane(k - 1, q);
+        const bool report = p.every > 0 && ((p.step0 + k) % p.every) == 0;
+        double acc_res = 0.0;
+        for (int lw = w_lo + warp; lw < w_hi; lw += kWarps) {
+          const int gw = gw0 + lw;
+          const bool w_in = gw >= 0 && gw < p.W;
+          const bool w_core = lw >= p.HW && lw < p.HW + p.TW;
+          for (int ld = d_lo + lane; ld < d_hi; ld += 32) {
+            const int gd = gd0 + ld;
+            const int idx = lw * LD + ld;
+            TS v;
+            if (w_in && gd >= 0 && gd < p.D) {
+              float acc = __fmul_rn(s_wt[0], S::load(nb[0][idx]));
+#pragma unroll
+              for (int n = 1; n < (NM > 0 ? NM : kMaxMask3D); ++n)
+                if (n < nm) acc = __fadd_rn(acc, __fmul_rn(s_wt[n], S::load(nb[n][idx])));
+              v = S::store(acc);
+              const bool core = w_core && ld >= p.HD && ld < p.HD + p.TD;
+              if (core) {
+                if (report) {
+                  const double dlt = static_cast<double>(S::load(v)) - static_cast<double>(S::load(prevp[idx]));
+                  acc_res += dlt * dlt;
+                }
+                if (k == steps) dst[(static_cast<int64_t>(q) * p.W + gw) * p.D + gd] = v;
+              }
+            } else {
+              v = halo;
+            }
+            if (k < steps) outp[idx] = v;
+          }
+        }
+        if (report) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc_res += __shfl_down_sync(0xFFFFFFFFu, acc_res, o);
+          if (lane == 0) s_part[k - 1][warp] += acc_res;
+        }
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- fp64 residual partials: one per (reported level, CTA)
+  if (p.every > 0 && tid == 0) {
+    for (int k = 1; k <= steps; ++k) {
+      if (((p.step0 + k) % p.every) != 0) continue;
+      double t = 0.0;
+      for (int w = 0; w < kWarps; ++w) t += s_part[k - 1][w];
+      p.partials[static_cast<size_t>(k - 1) * gridDim.x + blockIdx.x] = t;
+    }
+  }
+}
+
+// Sums the per-CTA partials of each reported step in CTA order and stores
+// the square root at residuals[slot0 + j].
+__global__ void reduce3d_residual(const double* __restrict__ partials, int nctas, int steps, int64_t step0, int every,
+                                  double* __restrict__ residuals) {
+  const int k = blockIdx.x + 1;  // level within the pass
+  if (k > steps || ((step0 + k) % every) != 0) return;
+  __shared__ double s[256];
+  double t = 0.0;
+  // fixed assignment of partials to threads and a fixed tree: deterministic
+  for (int c = threadIdx.x; c < nctas; c += blockDim.x) t += partials[static_cast<size_t>(k - 1) * nctas + c];
+  s[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) residuals[(step0 + k) / every - 1] = sqrt(s[0]);
+}
+
+template <class TS, int NM, bool kTma>
+cudaError_t launch3d(const CUtensorMap* map, const Stencil3DParams& p, int ctas, cudaStream_t s) {
+  const size_t smem = stencil3d_smem_bytes(p.TW + 2 * p.HW, p.TD + 2 * p.HD, p.NP, p.T, sizeof(TS));
+  auto kern = stencil3d_kernel<TS, NM, kTma>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  kern<<<ctas, kStencil3DThreads, smem, s>>>(*map, p);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || p.every <= 0) return e;
+  bool any = false;
+  for (int k = 1; k <= p.steps; ++k) any = any || ((p.step0 + k) % p.every) == 0;
+  if (!any) return cudaSuccess;
+  reduce3d_residual<<<p.steps, 256, 0, s>>>(p.partials, ctas, p.steps, p.step0, p.every, p.residuals);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize) {
+  const size_t pb = (static_cast<size_t>(LW) * LD * esize + 127) & ~size_t(127);
+  return 128 + (static_cast<size_t>(NP + 1) + static_cast<size_t>(T - 1) * NP) * pb + 16;
+}
+
+int stencil3d_max_ctas_per_sm(size_t smem) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int per_sm = 0, per_block = 0;
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem > static_cast<size_t>(per_block)) return 0;
+  const size_t static_smem = 3 * kMaxMask3D * 4 + 8 * 8 + 1024;
+  const int by_smem = static_cast<int>(per_sm / (smem + static_smem));
+  const int by_threads = 2048 / kStencil3DThreads;
+  return by_smem < by_threads ? by_smem : by_threads;
+}
+
+cudaError_t stencil3d_pass(int dtype, bool use_tma, const CUtensorMap* map_src, const Stencil3DParams& p, int ctas,
+                           cudaStream_t s) {
+  if (dtype == 2) {
+    if (use_tma)
+      return p.nm == 7 ? launch3d<__nv_bfloat16, 7, true>(map_src, p, ctas, s)
+                       : launch3d<__nv_bfloat16, 0, true>(map_src, p, ctas, s);
+    return p.nm == 7 ? launch3d<__nv_bfloat16, 7, false>(map_src, p, ctas, s)
+                     : launch3d<__nv_bfloat16, 0, false>(map_src, p, ctas, s);
+  }
+  if (use_tma)
+    return p.nm == 7 ? launch3d<float, 7, true>(map_src, p, ctas, s) : launch3d<float, 0, true>(map_src, p, ctas, s);
+  return p.nm == 7 ? launch3d<float, 7, false>(map_src, p, ctas, s) : launch3d<float, 0, false>(map_src, p, ctas, s);
+}
+
+}  // namespace pskel

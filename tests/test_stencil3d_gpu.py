@@ -1,0 +1,119 @@
+"""3D stencils on the GPU against the oracle.
+
+fp32 and bf16-storage grids are compared bit for bit (same operation order,
+no contraction, bf16 rounding every step). The fp64 residual norms are
+compared with a relative tolerance of 1e-12: the kernel sums per-CTA partials
+in a fixed order that differs from the oracle's serial order.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import pskel_gb300 as P
+from pskel_gb300 import synth as S
+from tests.gpu_util import bits
+
+pytestmark = pytest.mark.gpu
+
+RES_RTOL = 1e-12
+
+
+def grids(W, H, D, seed, dtype):
+    a, _ = S.heat3d(W, H, D, seed=seed)
+    b = S.uniform_f32(seed + 50, S.S_GRID, a.shape)  # the output's initial contents are never read
+    if dtype == "bf16":
+        return S.f32_to_bf16(a), S.f32_to_bf16(b)
+    return a, b
+
+
+def run3d(torch, st, a, b, iters, sched=None, every=0, dtype="f32"):
+    view = (lambda x: x.view(np.int16)) if dtype == "bf16" else (lambda x: x)
+    x = torch.from_numpy(view(np.ascontiguousarray(a))).cuda()
+    y = torch.from_numpy(view(np.ascontiguousarray(b))).cuda()
+    n = iters // every if every else 0
+    res = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+    P.iterate3d(st, x, y, iters, sched=sched, residual_every=every, residuals=res if every else None)
+    P.sync()
+    out = (y if iters % 2 == 1 else x).cpu().numpy()
+    if dtype == "bf16":
+        out = out.view(np.uint16)
+    return out, res.cpu().numpy()[:n]
+
+
+def heat(keep, dtype="f32", halo=0.0):
+    return P.make_stencil(P.OP_LINEAR, dtype, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, halo=halo, keep=keep)
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H,D", [(11, 9, 13), (32, 17, 64), (40, 33, 72), (1, 1, 1), (70, 5, 8)])
+@pytest.mark.parametrize("iters", [1, 2, 5])
+def test_heat3d_matches_oracle(cuda, oracle_mod, dtype, W, H, D, iters):
+    keep = P._Keep()
+    a, b = grids(W, H, D, W + H + D, dtype)
+    got, res = run3d(cuda, heat(keep, dtype, halo=0.5), a, b, iters, every=2, dtype=dtype)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, iters, halo=0.5, dtype=dtype, every=2)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
+
+
+@pytest.mark.parametrize("T,tw,td", [(1, 0, 0), (2, 16, 32), (3, 8, 16), (4, 32, 64), (8, 8, 8)])
+def test_heat3d_schedules(cuda, oracle_mod, T, tw, td):
+    keep = P._Keep()
+    a, b = grids(48, 31, 40, T, "f32")
+    sch = dict(time_steps=T, tile_w=tw, tile_h=0, tile_d=td, ctas=0)
+    got, res = run3d(cuda, heat(keep), a, b, 13, sched=sch, every=3)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 13, dtype="f32", every=3)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
+
+
+def test_general_3d_mask_radius2(cuda, oracle_mod):
+    keep = P._Keep()
+    off = [(0, 0, 0), (-2, 0, 0), (1, 1, 0), (0, -1, 2), (0, 0, -2), (2, -2, 1), (-1, 0, 1), (1, 0, -1), (0, 2, 0)]
+    wt = [0.3, 0.1, 0.05, 0.1, 0.15, 0.05, 0.1, 0.07, 0.08]
+    st = P.make_stencil(P.OP_LINEAR, "f32", off, wt, halo=-0.25, keep=keep)
+    a, b = grids(37, 23, 48, 3, "f32")
+    for iters in (1, 4, 7):
+        got, _ = run3d(cuda, st, a, b, iters)
+        want, _ = oracle_mod.lin3d(a, b, off, wt, iters, halo=-0.25)
+        assert np.array_equal(bits(got), bits(want))
+
+
+def test_heat3d_host_entry_point(cuda, oracle_mod):
+    keep = P._Keep()
+    for dtype in ("f32", "bf16"):
+        a, b = grids(64, 40, 64, 9, dtype)
+        a0 = a.copy()
+        out, res = P.run3d_host(heat(keep, dtype), a, b.copy(), 10, residual_every=5)
+        want, wres = oracle_mod.lin3d(a0, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 10, dtype=dtype, every=5)
+        assert np.array_equal(bits(out), bits(want))
+        np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
+        assert np.array_equal(a, a0)
+
+
+def test_heat3d_c4_size_vs_oracle_and_fp64_error(cuda, oracle_mod):
+    # 512^3: 10 steps against the fp32 oracle (and its residual), then the
+    # full 50 steps checked for schedule invariance, with the fp32 and bf16
+    # errors against the fp64 oracle on a 128^3 cut reported.
+    keep = P._Keep()
+    a, b = grids(512, 512, 512, 1, "f32")
+    got, res = run3d(cuda, heat(keep), a, b, 10, every=10)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 10, every=10)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
+    r2, n2 = run3d(cuda, heat(keep), a, b, 50, every=10, sched=dict(time_steps=2, tile_w=0, tile_h=0, tile_d=0, ctas=0))
+    r3, n3 = run3d(cuda, heat(keep), a, b, 50, every=10, sched=dict(time_steps=3, tile_w=16, tile_h=0, tile_d=32,
+                                                                     ctas=0))
+    assert np.array_equal(bits(r2), bits(r3))
+    np.testing.assert_allclose(n2, n3, rtol=RES_RTOL, atol=0)
+    assert np.all(np.diff(n2) < 0), "the heat equation's residual must decay"
+    c, d = grids(128, 128, 128, 2, "f32")
+    g32, _ = run3d(cuda, heat(keep), c, d, 50)
+    gb, _ = run3d(cuda, heat(keep, "bf16"), S.f32_to_bf16(c), S.f32_to_bf16(d), 50, dtype="bf16")
+    ref64, _ = oracle_mod.lin3d(c.astype(np.float64), d.astype(np.float64), S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 50,
+                                dtype="f64")
+    e32 = float(np.max(np.abs(g32 - ref64)))
+    eb = float(np.max(np.abs(S.bf16_to_f32(gb) - ref64)))
+    print(f"\nheat3d 128^3 x50: max abs error vs fp64: fp32 {e32:.3e}, bf16 storage {eb:.3e}")
+    assert e32 < 1e-5 and eb < 0.05

@@ -2,8 +2,9 @@
 
 fp32 and bf16-storage grids are compared bit for bit (same operation order,
 no contraction, bf16 rounding every step). The fp64 residual norms are
-compared with a relative tolerance of 1e-12: the kernel sums per-CTA partials
-in a fixed order that differs from the oracle's serial order.
+compared with a relative tolerance of 1e-12 plus the worst-case error of the
+oracle's own serial fp64 sum over n cells (n * 2^-53): the kernel adds per-CTA
+partials in a fixed tree, which is more accurate than the serial loop.
 """
 from __future__ import annotations
 
@@ -17,6 +18,10 @@ from tests.gpu_util import bits
 pytestmark = pytest.mark.gpu
 
 RES_RTOL = 1e-12
+
+
+def res_rtol(shape) -> float:
+    return RES_RTOL + float(np.prod(shape)) * 2.0**-53
 
 
 def grids(W, H, D, seed, dtype):
@@ -101,7 +106,7 @@ def test_heat3d_c4_size_vs_oracle_and_fp64_error(cuda, oracle_mod):
     got, res = run3d(cuda, heat(keep), a, b, 10, every=10)
     want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 10, every=10)
     assert np.array_equal(bits(got), bits(want))
-    np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
+    np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
     r2, n2 = run3d(cuda, heat(keep), a, b, 50, every=10, sched=dict(time_steps=2, tile_w=0, tile_h=0, tile_d=0, ctas=0))
     r3, n3 = run3d(cuda, heat(keep), a, b, 50, every=10, sched=dict(time_steps=3, tile_w=16, tile_h=0, tile_d=32,
                                                                      ctas=0))

@@ -48,6 +48,11 @@ WORKLOADS = {
                    W=4096, H=4096, iters=500, dtype="f32", T=4, b_alg=16),
     "advect_bf16": dict(desc="advection-diffusion 2D, bf16 storage / fp32 arithmetic, 4096x4096, 500 iterations",
                         W=4096, H=4096, iters=500, dtype="bf16", T=4, b_alg=8),
+    "heat3d": dict(desc="3D 7-point heat (Mask3D), float32 512^3, zero halo, 50 iterations, fp64 residual every 10",
+                   W=512, H=512, D=512, iters=50, dtype="f32", T=2, b_alg=8, every=10),
+    "heat3d_bf16": dict(desc="3D 7-point heat, bf16 storage / fp32 arithmetic, 512^3, 50 iterations, "
+                             "fp64 residual every 10", W=512, H=512, D=512, iters=50, dtype="bf16", T=2, b_alg=4,
+                        every=10),
 }
 
 
@@ -152,6 +157,11 @@ def make_inputs(wl):
         if wl["dtype"] == "bf16":
             a, b = S.f32_to_bf16(a), S.f32_to_bf16(b)
         return {"in": a, "out": b}
+    if name.startswith("heat3d"):
+        a, b = S.heat3d(W, H, wl["D"], seed=1)
+        if wl["dtype"] == "bf16":
+            a, b = S.f32_to_bf16(a), S.f32_to_bf16(b)
+        return {"in": a, "out": b}
     if name.startswith("advect"):
         a, b, u, v = S.advect2d(W, H, seed=1)
         if wl["dtype"] == "bf16":
@@ -166,6 +176,8 @@ def stencil_for(wl, P, S, keep, wind=(None, None)):
         return P.make_stencil(P.OP_LIFE, "u8", S.MOORE8_OFFSETS, keep=keep)
     if name.startswith("jacobi"):
         return P.make_stencil(P.OP_LINEAR, wl["dtype"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    if name.startswith("heat3d"):
+        return P.make_stencil(P.OP_LINEAR, wl["dtype"], S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, keep=keep)
     return P.make_stencil(P.OP_ADVECT, wl["dtype"], S.JACOBI4_OFFSETS, wind=wind, K=S.ADVECT_K, dt=S.ADVECT_DT,
                           inv_dx=S.ADVECT_INV_DX, keep=keep)
 
@@ -180,6 +192,7 @@ def run_ours(args, wl, world, rank, local):
     dev = torch.device("cuda", local)
     x = make_inputs(wl)
     W, H, iters = wl["W"], wl["H"], wl["iters"]
+    D = wl.get("D", 1)
     tview = (lambda a: torch.from_numpy(a.view(np.int16))) if wl["dtype"] == "bf16" else torch.from_numpy
     src0 = tview(x["in"]).to(dev)
     out0 = tview(x["out"]).to(dev)
@@ -195,8 +208,16 @@ def run_ours(args, wl, world, rank, local):
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)  # 512 MB > L2
 
+    is3d = "D" in wl
+    every = wl.get("every", 0)
+    res_dev = torch.zeros(max(1, iters // every if every else 1), dtype=torch.float64, device=dev)
+
     def one_step():
-        P.iterate2d(st, a, b, iters, sched=sch, stream=stream.cuda_stream)
+        if is3d:
+            P.iterate3d(st, a, b, iters, sched=sch, residual_every=every, residuals=res_dev if every else None,
+                        stream=stream.cuda_stream)
+        else:
+            P.iterate2d(st, a, b, iters, sched=sch, stream=stream.cuda_stream)
 
     def reset():
         with torch.cuda.stream(stream):
@@ -226,12 +247,15 @@ def run_ours(args, wl, world, rank, local):
     dist_barrier(world)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_dev = dist_max(sum(step_ms) / 1e3, world)
-    cells = W * H * iters
+    cells = W * H * D * iters
     value = world * cells * args.steps / t_dev / 1e9
 
     # result check against a schedule-independent property: the same run with
     # one generation per pass gives identical cells (the first step's result).
-    passes = P.lib.pskel_plan_passes(iters, sch.time_steps, None, 0)
+    if is3d:
+        passes = len(plan_any(iters, sch.time_steps))
+    else:
+        passes = P.lib.pskel_plan_passes(iters, sch.time_steps, None, 0)
     launches = passes * args.steps
 
     # kernel-only launch timing for the roofline: average pass duration
@@ -248,14 +272,26 @@ def run_ours(args, wl, world, rank, local):
         wind_host = (pu.data_ptr(), pv.data_ptr())
     st_h = stencil_for(wl, P, S, keep, wind_host)
     esz = pin_in.element_size()
-    h2d = W * H * esz * (3 if "u" in x else 1)
-    r = 1  # the output array's ring goes to the device too (read by every second step)
-    h2d += (2 * r * W + 2 * r * (H - 2 * r)) * esz
-    d2h = W * H * esz
+    if is3d:
+        h2d = W * H * D * esz  # the 3D output's initial contents are never read
+        d2h = W * H * D * esz + 8 * (iters // every if every else 0)
+    else:
+        h2d = W * H * esz * (3 if "u" in x else 1)
+        r = 1  # the output array's ring goes to the device too (read by every second step)
+        h2d += (2 * r * W + 2 * r * (H - 2 * r)) * esz
+        d2h = W * H * esz
+    res_host = np.zeros(max(1, iters // every if every else 1), dtype=np.float64)
+
+    def host_call():
+        if is3d:
+            return P.lib.pskel_run3d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, D, iters,
+                                          P.C.byref(sch), every, res_host.ctypes.data)
+        return P.lib.pskel_run2d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, iters,
+                                      P.C.byref(sch))
 
     def e2e_step():
         pin_out.copy_(pin_out0)
-        P.lib.pskel_run2d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, iters, P.C.byref(sch))
+        host_call()
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -263,28 +299,27 @@ def run_ours(args, wl, world, rank, local):
     for _ in range(args.steps):
         pin_out.copy_(pin_out0)
         t1 = time.perf_counter()
-        rc = P.lib.pskel_run2d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, iters,
-                                    P.C.byref(sch))
+        rc = host_call()
         times.append(time.perf_counter() - t1)
         if rc != 0:
             raise RuntimeError(P.lib.pskel_last_error().decode())
     t_e2e = dist_max(sum(times), world)
     e2e_value = world * cells * args.steps / t_e2e / 1e9
     # the e2e result equals the device-resident run's result
-    res_dev = (b if iters % 2 == 1 else a).cpu()
+    final_dev = (b if iters % 2 == 1 else a).cpu()
     # (the device run was reset between steps, so its final state is one run)
-    same = bool(torch.equal(res_dev, pin_out))
+    same = bool(torch.equal(final_dev, pin_out))
 
     peak, peak_kind = load_peaks()
     b_alg = wl["b_alg"]
-    achieved = b_alg * W * H * (iters / passes) / (per_launch_ms / 1e3) / 1e9
-    pass_bytes = b_alg * W * H  # the pass's own compulsory traffic: read + write the grid once
+    achieved = b_alg * W * H * D * (iters / passes) / (per_launch_ms / 1e3) / 1e9
+    pass_bytes = b_alg * W * H * D  # the pass's own compulsory traffic: read + write the grid once
     traffic = load_traffic(wl["name"])
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_dev / args.steps * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": wl["desc"], "grid": [H, W], "iterations_per_step": iters,
+        "config": {"workload": wl["desc"], "grid": [H, W, D] if is3d else [H, W], "iterations_per_step": iters,
                    "time_steps_per_pass": sch.time_steps, "l2": "flushed between timed steps (512 MB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": round(e2e_value, 3), "unit": "GCells/s", "h2d_bytes_per_step": h2d,
@@ -302,6 +337,17 @@ def run_ours(args, wl, world, rank, local):
         "wall_s": round(wall, 3),
     }
     return line, clk.summary()
+
+
+def plan_any(iters, T):
+    """Pass lengths of a 3D run (mirror of the library's plan for fully written grids)."""
+    p = [T] * (iters // T) + ([iters % T] if iters % T else [])
+    if len(p) % 2 != iters % 2:
+        for i, v in enumerate(p):
+            if v >= 2:
+                p[i:i + 1] = [v // 2, v - v // 2]
+                break
+    return p
 
 
 def load_traffic(name):
@@ -331,6 +377,12 @@ def cpu_sample(wl, threads, iters_sample, use_ref=True):
                 np.ascontiguousarray(v).tofile(d / k)
             if wl["name"] == "life":
                 cmd = ["life", W, H, iters_sample, threads, d / "in", d / "out", d / "res"]
+            elif wl["name"].startswith("heat3d"):
+                with open(d / "m.txt", "w") as f:
+                    f.write("7 3\n" + "".join(f"{o[0]} {o[1]} {o[2]} {w!r}\n" for o, w in zip(S.HEAT7_OFFSETS,
+                                                                                              S.HEAT7_WEIGHTS)))
+                cmd = ["lin3d", wl["dtype"], W, H, wl["D"], iters_sample, threads, d / "m.txt", "0.0", d / "in",
+                       d / "out", d / "res"]
             elif wl["name"].startswith("jacobi"):
                 with open(d / "m.txt", "w") as f:
                     f.write("4 2\n" + "".join(f"{o[0]} {o[1]} {w!r}\n" for o, w in zip(S.JACOBI4_OFFSETS,
@@ -343,7 +395,7 @@ def cpu_sample(wl, threads, iters_sample, use_ref=True):
                                  env=env, check=True).stdout
             wall = json.loads([l for l in out.splitlines() if l.startswith("{")][-1])["wall_s"]
             del npt
-        return W * H * iters_sample / wall / 1e9, "reference", wall
+        return W * H * wl.get("D", 1) * iters_sample / wall / 1e9, "reference", wall
     oracle.build()
     t0 = time.perf_counter()
     if wl["name"] == "life":
@@ -351,17 +403,21 @@ def cpu_sample(wl, threads, iters_sample, use_ref=True):
     elif wl["name"].startswith("jacobi"):
         from pskel_gb300 import synth as S
         oracle.lin2d(x["in"], x["out"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters_sample, dtype=wl["dtype"])
+    elif wl["name"].startswith("heat3d"):
+        from pskel_gb300 import synth as S
+        oracle.lin3d(x["in"], x["out"], S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, iters_sample, dtype=wl["dtype"])
     else:
         from pskel_gb300 import synth as S
         oracle.advect(x["in"], x["out"], x["u"], x["v"], iters_sample, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX,
                       dtype=wl["dtype"])
     wall = time.perf_counter() - t0
-    return W * H * iters_sample / wall / 1e9, "port", wall
+    return W * H * wl.get("D", 1) * iters_sample / wall / 1e9, "port", wall
 
 
 def sample_iters(wl):
-    # about 1e9 cell updates: a few seconds on the host cores
-    return max(1, int(1e9 // (wl["W"] * wl["H"])))
+    # about 1e9 cell updates (3D: 3e8): a few seconds on the host cores
+    cells = wl["W"] * wl["H"] * wl.get("D", 1)
+    return max(1, int((3e8 if "D" in wl else 1e9) // cells))
 
 
 def run_reference_arm(args, wl, world, rank):
@@ -376,9 +432,10 @@ def run_reference_arm(args, wl, world, rank):
         v, kind, w = cpu_sample(wl, threads, its)
         vals.append(v)
         walls.append(w)
-    cells = wl["W"] * wl["H"] * its * args.steps
+    cells = wl["W"] * wl["H"] * wl.get("D", 1) * its * args.steps
     value = cells / sum(walls) / 1e9
-    sample = f"{wl['H']}x{wl['W']} grid, {its} iterations per step (of {wl['iters']}), {threads} OpenMP threads"
+    shape = "x".join(str(v) for v in ([wl["H"], wl["W"]] + ([wl["D"]] if "D" in wl else [])))
+    sample = f"{shape} grid, {its} iterations per step (of {wl['iters']}), {threads} OpenMP threads"
     return {"metric": METRIC, "value": round(value, 4), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(sum(walls) / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",

@@ -163,6 +163,27 @@ PSKEL_API pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_
                                         const pskel_schedule* sched, int64_t residual_every,
                                         double* residuals_host);
 
+/* pskel_iterate3d without any allocation by the library. It has no
+ * counterpart in the reference: it serves callers that cannot let a library
+ * call cudaMalloc, such as a host application that owns all device memory
+ * through its own pool, or a latency-critical loop that cannot absorb
+ * cudaMalloc's implicit synchronisation. The residual scratch and the device
+ * error word live in file-scope device arrays of fixed size, held by every GPU
+ * that loads the library until the process exits: at most 16384 fp64 partial
+ * sums (time_steps x CTAs of one pass); larger schedules are rejected with
+ * PSKEL_ERR_UNSUPPORTED (lower schedule.ctas or time_steps). The first call on
+ * a device looks up the arrays' device addresses; make that first call before
+ * any stream capture. All calls on a device share its arrays and the arrays
+ * keep the last call's contents: calls that overlap on the GPU (for example on
+ * two streams of one device) race. Every pass rewrites all the partials it
+ * reads, and a reported error word is cleared, so nothing else needs clearing. The
+ * caller passes the grids and the residual output, as for pskel_iterate3d.
+ * Synchronous: it waits for `stream` and reports kernel-side errors. */
+PSKEL_API pskel_status pskel_iterate3d_noalloc(const pskel_stencil* st, void* in, void* out, int64_t width,
+                                               int64_t height, int64_t depth, int64_t iterations,
+                                               const pskel_schedule* sched, int64_t residual_every,
+                                               double* residuals, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,9 @@ def _load():
                                      C.POINTER(Schedule)]
     lib.pskel_iterate3d.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                     C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p, C.c_void_p]
+    lib.pskel_iterate3d_noalloc.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                            C.c_int64, C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p,
+                                            C.c_void_p]
     lib.pskel_run3d_host.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                      C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p]
     return lib

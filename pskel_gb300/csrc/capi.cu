@@ -445,7 +445,7 @@ pskel_status validate3d(const pskel_stencil* st, const void* in, const void* out
   return PSKEL_OK;
 }
 
-static pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
+pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
                               int64_t iters, int R, const pskel_schedule* sched, int64_t every, double* residuals,
                               double* partials_override, int64_t partials_cap, DeviceContext* c, cudaStream_t s) {
   const int dtype = static_cast<int>(st.dtype);

@@ -32,5 +32,13 @@ pskel_status get_context(DeviceContext** out);
 pskel_status ensure_buffer(DeviceBuffer& b, size_t bytes);
 pskel_status device_sync_check(DeviceContext* c, cudaStream_t s);
 pskel_status check_mask(const pskel_mask& m, int dim, bool need_weights, int* max_off, int* ring);
+pskel_status validate3d(const pskel_stencil* st, const void* in, const void* out, int64_t W, int64_t H, int64_t D,
+                        int64_t iters, int64_t every, int* R);
+// The 3D pass loop. With partials_override set, the residual partial sums go
+// to that array (capacity partials_cap doubles) instead of c->partials, and
+// nothing is allocated.
+pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D, int64_t iters,
+                       int R, const pskel_schedule* sched, int64_t every, double* residuals, double* partials_override,
+                       int64_t partials_cap, DeviceContext* c, cudaStream_t s);
 
 }  // namespace pskel

@@ -1,0 +1,177 @@
+// A PSkel application written against the reference's API, built on the
+// GB300 drop-in headers. Used by tests/test_dropin_gpu.py.
+//
+//   dropin_app SCENARIO W H D ITERS IN OUTINIT RESULT [RESIDUALS]
+//
+// Grids are raw files in the reference's layouts; D is 1 for 2D scenarios.
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "PSkel.h"
+
+using namespace PSkel;
+
+struct JacobiLib : LinearStencil {};
+struct JacobiUser {
+  int unused;
+};
+struct LifeLib : LifeStencil {};
+struct LifeUser {
+  int unused;
+};
+struct HeatLib : LinearStencil {};
+struct HeatUser {
+  int unused;
+};
+
+namespace PSkel {
+// weighted sum in mask order (the linear stencil's definition)
+__parallel__ void stencilKernel(Array2D<float> in, Array2D<float> out, Mask2D<float> mask, JacobiLib, size_t h,
+                                size_t w) {
+  float acc = mask.getWeight(0) * mask.get(0, in, h, w);
+  for (size_t n = 1; n < mask.size; ++n) acc = acc + mask.getWeight(n) * mask.get(n, in, h, w);
+  out(h, w) = acc;
+}
+__parallel__ void stencilKernel(Array2D<float> in, Array2D<float> out, Mask2D<float> mask, JacobiUser, size_t h,
+                                size_t w) {
+  float acc = mask.getWeight(0) * mask.get(0, in, h, w);
+  for (size_t n = 1; n < mask.size; ++n) acc = acc + mask.getWeight(n) * mask.get(n, in, h, w);
+  out(h, w) = acc;
+}
+__parallel__ void stencilKernel(Array2D<uint8_t> in, Array2D<uint8_t> out, Mask2D<uint8_t> mask, LifeUser, size_t h,
+                                size_t w) {
+  int s = 0;
+  for (size_t n = 0; n < mask.size; ++n) s += mask.get(n, in, h, w);
+  const uint8_t c = in(h, w);
+  out(h, w) = (s == 3 || (s == 2 && c == 1)) ? 1 : 0;
+}
+__parallel__ void stencilKernel(Array2D<uint8_t> in, Array2D<uint8_t> out, Mask2D<uint8_t> mask, LifeLib, size_t h,
+                                size_t w) {
+  stencilKernel(in, out, mask, LifeUser{0}, h, w);
+}
+__parallel__ void stencilKernel(Array3D<float> in, Array3D<float> out, Mask3D<float> mask, HeatUser, size_t h,
+                                size_t w, size_t d) {
+  float acc = mask.getWeight(0) * mask.get(0, in, h, w, d);
+  for (size_t n = 1; n < mask.size; ++n) acc = acc + mask.getWeight(n) * mask.get(n, in, h, w, d);
+  out(h, w, d) = acc;
+}
+__parallel__ void stencilKernel(Array3D<float> in, Array3D<float> out, Mask3D<float> mask, HeatLib, size_t h, size_t w,
+                                size_t d) {
+  stencilKernel(in, out, mask, HeatUser{0}, h, w, d);
+}
+}  // namespace PSkel
+
+template <class T>
+static void read_raw(const char* path, T* dst, size_t n) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f || std::fread(dst, sizeof(T), n, f) != n) {
+    std::fprintf(stderr, "cannot read %s\n", path);
+    std::exit(2);
+  }
+  std::fclose(f);
+}
+template <class T>
+static void write_raw(const char* path, const T* src, size_t n) {
+  FILE* f = std::fopen(path, "wb");
+  if (!f || std::fwrite(src, sizeof(T), n, f) != n) {
+    std::fprintf(stderr, "cannot write %s\n", path);
+    std::exit(2);
+  }
+  std::fclose(f);
+}
+
+static Mask2D<float> jacobi_mask() {
+  Mask2D<float> m(4);
+  m.set(0, -1, 0, 0.25f);
+  m.set(1, 1, 0, 0.25f);
+  m.set(2, 0, -1, 0.25f);
+  m.set(3, 0, 1, 0.25f);
+  return m;
+}
+
+static Mask3D<float> heat_mask(float halo) {
+  Mask3D<float> m(7, halo);
+  const int off[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+  for (int n = 0; n < 7; ++n) m.set(n, off[n][0], off[n][1], off[n][2], n == 0 ? 0.25f : 0.125f);
+  return m;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 9) {
+    std::fprintf(stderr, "usage: dropin_app SCENARIO W H D ITERS IN OUTINIT RESULT [RESIDUALS]\n");
+    return 2;
+  }
+  const std::string sc = argv[1];
+  const size_t W = std::strtoull(argv[2], 0, 10), H = std::strtoull(argv[3], 0, 10), D = std::strtoull(argv[4], 0, 10);
+  const size_t it = std::strtoull(argv[5], 0, 10);
+  const char *fin = argv[6], *fout = argv[7], *fres = argv[8];
+
+  if (sc.rfind("jacobi", 0) == 0) {
+    Array2D<float> in(W, H), out(W, H);
+    read_raw(fin, in.hostArray, W * H);
+    read_raw(fout, out.hostArray, W * H);
+    Mask2D<float> mask = jacobi_mask();
+    if (sc == "jacobi_lib") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiLib> st(in, out, mask, JacobiLib());
+      st.runIterativeGPU(it, 32, 4);
+    } else if (sc == "jacobi_pyramid") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiLib> st(in, out, mask, JacobiLib());
+      st.runIterativeGPU(it, 3, 32, 4);
+    } else if (sc == "jacobi_tiling") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiLib> st(in, out, mask, JacobiLib());
+      st.runIterativeTilingGPU(it, 64, 32, 1, 5);
+    } else if (sc == "jacobi_auto") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiLib> st(in, out, mask, JacobiLib());
+      st.runIterativeAutoGPU(it);
+    } else if (sc == "jacobi_user") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
+      st.runIterativeGPU(it, 0, 0);
+    } else if (sc == "jacobi_cpu") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
+      st.runIterativeCPU(it, 4);
+    } else {
+      return 3;
+    }
+    write_raw(fres, out.hostArray, W * H);
+  } else if (sc.rfind("life", 0) == 0) {
+    Array2D<uint8_t> in(W, H), out(W, H);
+    read_raw(fin, in.hostArray, W * H);
+    read_raw(fout, out.hostArray, W * H);
+    int moore[8][2] = {{-1, -1}, {-1, 0}, {-1, 1}, {0, -1}, {0, 1}, {1, -1}, {1, 0}, {1, 1}};
+    Mask2D<uint8_t> mask(8, moore);
+    if (sc == "life_lib") {
+      Stencil2D<Array2D<uint8_t>, Mask2D<uint8_t>, LifeLib> st(in, out, mask, LifeLib());
+      st.runIterativeGPU(it, 32, 4);
+    } else if (sc == "life_user") {
+      Stencil2D<Array2D<uint8_t>, Mask2D<uint8_t>, LifeUser> st(in, out, mask, LifeUser{0});
+      st.runIterativeGPU(it, 7, 32, 4);
+    } else {
+      return 3;
+    }
+    write_raw(fres, out.hostArray, W * H);
+  } else if (sc.rfind("heat", 0) == 0) {
+    Array3D<float> in(W, H, D), out(W, H, D);
+    read_raw(fin, in.hostArray, W * H * D);
+    read_raw(fout, out.hostArray, W * H * D);
+    Mask3D<float> mask = heat_mask(0.5f);
+    if (sc == "heat_lib") {
+      Stencil3D<Array3D<float>, Mask3D<float>, HeatLib> st(in, out, mask, HeatLib());
+      st.setResidualInterval(2);
+      st.runIterativeGPU(it, 0, 0);
+      if (argc > 9) write_raw(argv[9], st.residuals().data(), st.residuals().size());
+    } else if (sc == "heat_user") {
+      Stencil3D<Array3D<float>, Mask3D<float>, HeatUser> st(in, out, mask, HeatUser{0});
+      st.runIterativeGPU(it, 0, 0);
+    } else {
+      return 3;
+    }
+    write_raw(fres, out.hostArray, W * H * D);
+  } else {
+    return 3;
+  }
+  std::printf("ok %s\n", sc.c_str());
+  return 0;
+}

@@ -279,10 +279,104 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
   return PSKEL_OK;
 }
 
+static bool tma_ok(const void* p, int64_t pitch_bytes);
+
+// The register-windowed kernel (stencil2d_fast.cu) for reach-1 masks of a
+// known shape and for advection, when every buffer can be staged by TMA.
+static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, void* out, int64_t W, int64_t H,
+                                   int64_t pitch, int64_t iters, int ring, const pskel_schedule* sched,
+                                   DeviceContext* c, cudaStream_t s, bool* used) {
+  *used = false;
+  const bool advect = st.op == PSKEL_OP_ADVECT;
+  const int dtype = static_cast<int>(st.dtype);
+  const int N = 4;                 // cells per thread vector
+  const int vec = (dtype == PSKEL_BF16) ? 8 : 4;  // TMA x alignment (16 bytes) in cells
+  const int LW = 128;
+  const int S = (sched && sched->tile_h > 64) ? 8 : 4;
+  const int LH = 16 * S + 2;
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : (dtype == PSKEL_BF16 ? 7 : 3);
+  T = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(iters, 1)));
+  if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
+  int HX = 0, HY = 0;
+  for (;;) {
+    HY = T;
+    HX = ((T + vec - 1) / vec) * vec;
+    if ((LW - 2 * HX >= N && LH - 2 * HY >= 2) || T == 1) break;
+    T -= 2;
+  }
+  const size_t smem = fast2d_smem_bytes(advect, dtype, S);
+  if (smem > static_cast<size_t>(c->smem_optin)) return PSKEL_OK;
+  const int64_t pb = pitch * static_cast<int64_t>(dtype == PSKEL_BF16 ? 2 : 4);
+  bool ok = tma_ok(in, pb) && tma_ok(out, pb);
+  if (advect) ok = ok && tma_ok(st.wind_u, pb) && tma_ok(st.wind_v, pb);  // vector loads of the winds
+  if (!ok) return PSKEL_OK;
+  Stencil2DParams p;
+  memset(&p, 0, sizeof(p));
+  p.W = static_cast<int>(W);
+  p.H = static_cast<int>(H);
+  p.pitch = pitch;
+  p.ring = ring;
+  p.R = 1;
+  p.T = T;
+  p.TW = LW - 2 * HX;
+  p.TH = LH - 2 * HY;
+  p.LW = LW;
+  p.LH = LH;
+  p.HX = HX;
+  p.HY = HY;
+  p.tiles_x = static_cast<int>((W + p.TW - 1) / p.TW);
+  p.tiles_y = static_cast<int>((H + p.TH - 1) / p.TH);
+  p.err = c->err;
+  if (advect) {
+    p.K = st.diffusivity;
+    p.dt = st.dt;
+    p.inv_dx = st.inv_dx;
+  } else {
+    p.nm = st.mask.size;
+    for (int n = 0; n < p.nm; ++n) p.wt[n] = st.mask.weights[n];
+  }
+  const int ntiles = p.tiles_x * p.tiles_y;
+  const int per_sm = std::max(1, fast2d_max_ctas_per_sm(advect, dtype, S));
+  int ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
+  ctas = std::max(1, std::min(ctas, ntiles));
+  const CUtensorMapDataType tt = (dtype == PSKEL_BF16) ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const uint64_t dims[2] = {static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
+  const uint64_t strides[1] = {static_cast<uint64_t>(pb)};
+  const uint32_t box[2] = {static_cast<uint32_t>(LW), static_cast<uint32_t>(LH)};
+  CUtensorMap m_in, m_out, m_u, m_v;
+  memset(&m_u, 0, sizeof(m_u));
+  memset(&m_v, 0, sizeof(m_v));
+  cudaError_t e = encode_tmap(&m_in, tt, 2, in, dims, strides, box);
+  if (e == cudaSuccess) e = encode_tmap(&m_out, tt, 2, out, dims, strides, box);
+  if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled");
+  if (advect) {
+    p.u = st.wind_u;
+    p.v = st.wind_v;
+  }
+  *used = true;
+  const std::vector<int> passes = plan_passes(iters, T);
+  for (size_t i = 0; i < passes.size(); ++i) {
+    const bool fwd = (i % 2 == 0);
+    p.src = fwd ? in : out;
+    p.dst = fwd ? out : in;
+    p.steps = passes[i];
+    e = fast2d_pass(opk, dtype, S, fwd ? &m_in : &m_out, fwd ? &m_out : &m_in, &m_u, &m_v, p, ctas, s);
+    if (e != cudaSuccess) return cuda_fail(e, "2D stencil kernel launch");
+  }
+  return PSKEL_OK;
+}
+
 static pskel_status iterate_float2d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
                                     int64_t iters, int R, int ring, const pskel_schedule* sched, DeviceContext* c,
                                     cudaStream_t s) {
   const Op2D op = (st.op == PSKEL_OP_ADVECT) ? Op2D::Advect : Op2D::Linear;
+  const int opk = (op == Op2D::Advect) ? 3 : (R == 1 ? fast2d_shape(st.mask.offsets, st.mask.size) : -1);
+  const bool generic_requested = sched && sched->tile_w > 0;  // explicit tile widths select the generic kernel
+  if (opk >= 0 && !generic_requested) {
+    bool used = false;
+    if (pskel_status q = iterate_fast2d(st, opk, in, out, W, H, pitch, iters, ring, sched, c, s, &used)) return q;
+    if (used) return PSKEL_OK;
+  }
   const int dtype = static_cast<int>(st.dtype);
   const size_t esz = dtype_size(st.dtype);
   const int vec = static_cast<int>(16 / esz);

@@ -81,6 +81,18 @@ cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* 
                            const CUtensorMap* map_u,
                            const CUtensorMap* map_v, const Stencil2DParams& p, int ctas, cudaStream_t s);
 
+// Register-windowed 2D kernel for reach-1 masks of a known shape and for
+// advection. Shapes (entries in summation order): 0 = N,S,W,E;
+// 1 = C,N,S,W,E; 2 = the 3x3 box row by row. Returns -1 for other masks.
+int fast2d_shape(const int* offsets, int n);
+size_t fast2d_smem_bytes(bool advect, int dtype, int S);
+int fast2d_max_ctas_per_sm(bool advect, int dtype, int S);
+// opk: a shape above, or 3 for advection. Tile: 128 cells wide, 16 * S + 2
+// rows high (S = 4 or 8), 512 threads.
+cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const CUtensorMap* md,
+                        const CUtensorMap* mu, const CUtensorMap* mv, const Stencil2DParams& p, int ctas,
+                        cudaStream_t s);
+
 // ------------------------------------------------------- 3D float stencils
 
 constexpr int kMaxMask3D = 32;

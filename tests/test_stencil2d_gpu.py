@@ -170,3 +170,34 @@ def test_jacobi_c1_full_size_and_fp64_error(cuda, oracle_mod):
     # bf16 keeps 8 significand bits: each stored step rounds by up to 2^-9
     # relative, so 100 steps on values in [0, 1) stay well inside 0.1
     assert err32 < 1e-5 and errb < 0.1
+
+
+CROSS5_OFFSETS = [(0, 0), (-1, 0), (1, 0), (0, -1), (0, 1)]
+CROSS5_WEIGHTS = [0.2, 0.3, 0.1, 0.25, 0.15]
+BOX9_OFFSETS = [(-1, -1), (-1, 0), (-1, 1), (0, -1), (0, 0), (0, 1), (1, -1), (1, 0), (1, 1)]
+BOX9_WEIGHTS = [0.05, 0.1, 0.05, 0.15, 0.3, 0.15, 0.05, 0.1, 0.05]
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("offsets,weights", [(S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS), (CROSS5_OFFSETS, CROSS5_WEIGHTS),
+                                             (BOX9_OFFSETS, BOX9_WEIGHTS)])
+@pytest.mark.parametrize("T,th", [(0, 0), (1, 0), (3, 0), (5, 100), (7, 100), (15, 100)])
+def test_register_windowed_shapes(cuda, oracle_mod, dtype, offsets, weights, T, th):
+    # known reach-1 shapes with a 16-byte aligned pitch take the register-windowed kernel
+    keep = P._Keep()
+    if dtype == "bf16":
+        weights = [float(S.bf16_to_f32(S.f32_to_bf16(np.array([w], np.float32)))[0]) for w in weights]
+    st = P.make_stencil(P.OP_LINEAR, dtype, offsets, weights, keep=keep)
+    a, b = jac_grids(517, 389, T + 11, dtype)
+    got = run2d(cuda, st, a, b, 19, sched=sched(T, 0, th), dtype=dtype)
+    want = oracle_mod.lin2d(a, b, offsets, weights, 19, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("T,th", [(0, 0), (1, 0), (5, 100)])
+def test_advection_register_windowed(cuda, oracle_mod, dtype, T, th):
+    a, b, u, v = _advect_inputs(700, 333, 6, dtype)
+    got = _advect_gpu(cuda, dtype, a, b, u, v, 17, sch=sched(T, 0, th))
+    want = oracle_mod.advect(a, b, u, v, 17, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))

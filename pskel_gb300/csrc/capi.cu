@@ -580,6 +580,19 @@ pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, 
   p.HD = HD;
   p.tiles_w = static_cast<int>((W + TW - 1) / TW);
   p.tiles_d = static_cast<int>((D + TD - 1) / TD);
+  // chunks of h: enough work items for every resident CTA, each long enough
+  // that the warm-up planes (steps * R per chunk) stay a small fraction
+  {
+    const int cols = p.tiles_w * p.tiles_d;
+    const int per_sm0 = std::max(1, stencil3d_max_ctas_per_sm(smem));
+    const int want = 2 * per_sm0 * c->sms;
+    int chunks = std::max(1, (want + cols - 1) / cols);
+    const int min_planes = std::max(16, 8 * R * T);
+    chunks = static_cast<int>(std::min<int64_t>(chunks, std::max<int64_t>(1, H / min_planes)));
+    if (sched && sched->tile_h > 0) chunks = static_cast<int>(std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h));
+    p.HC = static_cast<int>((H + chunks - 1) / chunks);
+    p.hchunks = static_cast<int>((H + p.HC - 1) / p.HC);
+  }
   p.nm = st.mask.size;
   for (int n = 0; n < p.nm; ++n) {
     p.off_h[n] = st.mask.offsets[3 * n];
@@ -590,7 +603,7 @@ pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, 
   p.err = c->err;
   p.every = static_cast<int>(every);
   p.residuals = residuals;
-  const int ntiles = p.tiles_w * p.tiles_d;
+  const int ntiles = p.tiles_w * p.tiles_d * p.hchunks;
   const int per_sm = std::max(1, stencil3d_max_ctas_per_sm(smem));
   int ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
   ctas = std::max(1, std::min(ctas, ntiles));

@@ -108,6 +108,7 @@ struct Stencil3DParams {
   int LW, LD;         // plane window
   int HW, HD;         // halos in w and d
   int tiles_w, tiles_d;
+  int HC, hchunks;    // output planes per work item, work items along h
   int nm;
   int off_h[kMaxMask3D];      // dh per entry
   int off_plane[kMaxMask3D];  // dw * LD + dd per entry

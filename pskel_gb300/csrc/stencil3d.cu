@@ -81,14 +81,22 @@ __global__ void __launch_bounds__(kStencil3DThreads)
   const TS halo = S::store(p.halo);
   const TS* src = static_cast<const TS*>(p.src);
   TS* dst = static_cast<TS*>(p.dst);
-  const int ntiles = p.tiles_w * p.tiles_d;
+  const int ncols = p.tiles_w * p.tiles_d;
+  const int ntiles = ncols * p.hchunks;
   const int steps = p.steps;
   uint32_t phase = 0;
 
-  const int last = p.H - 1 + steps * R;  // march positions 0..last
+  // Work items: a (w, d) tile column over a chunk [h0, h1) of output planes.
+  // The march starts steps * R planes early to warm the level rings up.
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int tw = tile / p.tiles_d;
-    const int td = tile - tw * p.tiles_d;
+    const int hc = tile / ncols;
+    const int col = tile - hc * ncols;
+    const int tw = col / p.tiles_d;
+    const int td = col - tw * p.tiles_d;
+    const int h0 = hc * p.HC;
+    const int h1 = min(p.H, h0 + p.HC);
+    const int first = max(0, h0 - steps * R);
+    const int last = h1 - 1 + steps * R;
     const int gw0 = tw * p.TW - p.HW;  // global w of local w 0
     const int gd0 = td * p.TD - p.HD;  // global d of local d 0
     const bool edge = (gw0 < 0) || (gw0 + LW > p.W) || (gd0 < 0) || (gd0 + LD > p.D);
@@ -103,9 +111,9 @@ __global__ void __launch_bounds__(kStencil3DThreads)
       mbar_arrive_expect_tx(bar, static_cast<uint32_t>(plane_elems * sizeof(TS)));
       tma_load_3d(level_plane(0, plane), &map_src, gd0, gw0, plane, bar);
     };
-    if (kTma && tid == 0 && p.H > 0) issue(0);
+    if (kTma && tid == 0 && first < p.H) issue(first);
 
-    for (int i = 0; i <= last; ++i) {
+    for (int i = first; i <= last; ++i) {
       // ---- level 0: input plane i
       if (i < p.H && !kTma) {
         TS* pl = level_plane(0, i);
@@ -131,12 +139,13 @@ __global__ void __launch_bounds__(kStencil3DThreads)
       }
       __syncthreads();
       // the slot of plane i+1 held plane i-NP-... no longer read: prefetch it
-      if (kTma && tid == 0 && i + 1 < p.H) issue(i + 1);
+      if (kTma && tid == 0 && i + 1 < p.H && i + 1 <= last) issue(i + 1);
 
       // ---- levels 1..steps
       for (int k = 1; k <= steps; ++k) {
         const int q = i - k * R;
-        if (q < 0) continue;
+        // planes this level must produce for the chunk's output planes
+        if (q < max(0, h0 - (steps - k) * R) || q >= h1 + (steps - k) * R) continue;
         if (k < steps && q >= p.H) {
           fill_plane(level_plane(k, q), plane_elems, halo);
           __syncthreads();
@@ -153,7 +162,8 @@ __global__ void __launch_bounds__(kStencil3DThreads)
           if (n < nm) nb[n] = level_plane(k - 1, q + s_offh[n]) + s_offp[n];
         TS* outp = (k < steps) ? level_plane(k, q) : nullptr;
         const TS* prevp = level_plane(k - 1, q);
-        const bool report = p.every > 0 && ((p.step0 + k) % p.every) == 0;
+        // the chunk owns planes [h0, h1): only those count in the residual
+        const bool report = p.every > 0 && ((p.step0 + k) % p.every) == 0 && q >= h0 && q < h1;
         double acc_res = 0.0;
         for (int lw = w_lo + warp; lw < w_hi; lw += kWarps) {
           const int gw = gw0 + lw;

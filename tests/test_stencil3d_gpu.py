@@ -62,11 +62,13 @@ def test_heat3d_matches_oracle(cuda, oracle_mod, dtype, W, H, D, iters):
     np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
 
 
-@pytest.mark.parametrize("T,tw,td", [(1, 0, 0), (2, 16, 32), (3, 8, 16), (4, 32, 64), (8, 8, 8)])
-def test_heat3d_schedules(cuda, oracle_mod, T, tw, td):
+@pytest.mark.parametrize("T,tw,td,th", [(1, 0, 0, 0), (2, 16, 32, 0), (3, 8, 16, 5), (4, 32, 64, 7), (8, 8, 8, 0),
+                                        (2, 0, 0, 1), (3, 16, 16, 13)])
+def test_heat3d_schedules(cuda, oracle_mod, T, tw, td, th):
+    # th: output planes per work item along h (chunks with warm-up planes)
     keep = P._Keep()
     a, b = grids(48, 31, 40, T, "f32")
-    sch = dict(time_steps=T, tile_w=tw, tile_h=0, tile_d=td, ctas=0)
+    sch = dict(time_steps=T, tile_w=tw, tile_h=th, tile_d=td, ctas=0)
     got, res = run3d(cuda, heat(keep), a, b, 13, sched=sch, every=3)
     want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 13, dtype="f32", every=3)
     assert np.array_equal(bits(got), bits(want))

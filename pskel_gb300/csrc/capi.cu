@@ -93,6 +93,7 @@ pskel_status device_sync_check(DeviceContext* c, cudaStream_t s) {
     if (word & kDevErrTimeout) msg += " a TMA/mbarrier wait timed out;";
     if (word & kDevErrValue) msg += " a Life cell outside {0,1};";
     if (word & kDevErrBarrier) msg += " a batched-schedule dependency wait timed out;";
+    if (word & kDevErrAlign) msg += " dynamic shared memory was not 128-byte aligned;";
     return fail(PSKEL_ERR_DEVICE, "%s", msg.c_str());
   }
   return PSKEL_OK;

@@ -14,6 +14,7 @@ enum DeviceError : unsigned {
   kDevErrTimeout = 1u,    // an mbarrier wait ran out of iterations
   kDevErrValue = 2u,      // an input value outside the kernel's domain (Life: cell not 0/1)
   kDevErrBarrier = 4u,    // a batched-schedule dependency wait ran out of iterations
+  kDevErrAlign = 8u,      // dynamic shared memory not 128-byte aligned (kernel did nothing)
 };
 
 // Upper bound on mbarrier polls before a kernel gives up on a TMA load. A load

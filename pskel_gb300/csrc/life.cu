@@ -127,8 +127,15 @@ __global__ void __launch_bounds__(kLifeThreads, 3)
     life_kernel(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap map_dst,
                 const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int W, int H, int64_t pitch, int ring,
                 int steps, int T, int TH, int LH, int tiles_x, int tiles_y, unsigned* err) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // dynamic shared memory, 128-byte aligned for TMA; derived pointers stay
+  // in the shared window (no integer round trip), so accesses compile to
+  // shared-memory instructions
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  uint8_t* slots = smem_raw;
+  if ((smem_u32(smem_raw) & 127u) != 0) {
+    if (threadIdx.x == 0) atomicOr(err, kDevErrAlign);
+    return;
+  }
   uint32_t* bitsA = reinterpret_cast<uint32_t*>(slots + kSlots * kChunkRows * kLifeLW);
   uint32_t* bitsB = bitsA + kBitPlaneWords;
   uint64_t* bars = reinterpret_cast<uint64_t*>(bitsB + kBitPlaneWords);

@@ -94,8 +94,15 @@ __global__ void __launch_bounds__(kStencil2DThreads)
                      const __grid_constant__ CUtensorMap map_v, const __grid_constant__ Stencil2DParams p) {
   using S = Storage<TS>;
   using L = Layout<TS, OP>;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // dynamic shared memory, 128-byte aligned for TMA; derived pointers stay
+  // in the shared window (no integer round trip), so accesses compile to
+  // shared-memory instructions
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  uint8_t* base = smem_raw;
+  if ((smem_u32(smem_raw) & 127u) != 0) {
+    if (threadIdx.x == 0) atomicOr(p.err, kDevErrAlign);
+    return;
+  }
   const int LW = p.LW, LH = p.LH;
   const size_t bb = L::buf_bytes(LW, LH);
   TS* bufA = reinterpret_cast<TS*>(base);

@@ -117,8 +117,15 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   constexpr bool kAdvect = (OpK == 3);
   constexpr size_t kBuf = (static_cast<size_t>(LW) * LH * sizeof(TS) + 127) & ~size_t(127);
   constexpr uint32_t kTileBytes = static_cast<uint32_t>(LW * LH * sizeof(TS));
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // dynamic shared memory, 128-byte aligned for TMA; derived pointers stay
+  // in the shared window (no integer round trip), so accesses compile to
+  // shared-memory instructions
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  uint8_t* base = smem_raw;
+  if ((smem_u32(smem_raw) & 127u) != 0) {
+    if (threadIdx.x == 0) atomicOr(p.err, kDevErrAlign);
+    return;
+  }
   auto buf = [&](int i) { return reinterpret_cast<TS*>(base + static_cast<size_t>(i) * kBuf); };
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + kFastBufs * kBuf);  // one per buffer
   (void)map_u;

@@ -40,23 +40,23 @@ template <class TS, int NM, bool kTma>
 __global__ void __launch_bounds__(kStencil3DThreads)
     stencil3d_kernel(const __grid_constant__ CUtensorMap map_src, const __grid_constant__ Stencil3DParams p) {
   using S = Storage<TS>;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // dynamic shared memory, 128-byte aligned for TMA; planes are addressed by
+  // element offsets from `sm`, so every access is a shared-memory access
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  if ((smem_u32(smem_raw) & 127u) != 0) {
+    if (threadIdx.x == 0) atomicOr(p.err, kDevErrAlign);
+    return;
+  }
+  TS* sm = reinterpret_cast<TS*>(smem_raw);
   const int LW = p.LW, LD = p.LD, NP = p.NP, R = p.R;
   const int plane_elems = LW * LD;
-  const size_t pb = plane_bytes<TS>(LW, LD);
+  const int pe = static_cast<int>(plane_bytes<TS>(LW, LD) / sizeof(TS));  // plane stride in elements
   // level 0 ring has one extra slot so the next plane can load while the
   // current ones are still read; levels 1..steps-1 have NP slots each
   const int NP0 = NP + 1;
-  TS* lvl0 = reinterpret_cast<TS*>(base);
-  auto level_plane = [&](int k, int q) -> TS* {
-    if (k == 0) return reinterpret_cast<TS*>(base + static_cast<size_t>((q % NP0 + NP0) % NP0) * pb);
-    return reinterpret_cast<TS*>(base + (NP0 + static_cast<size_t>(k - 1) * NP + (q % NP + NP) % NP) * pb);
-  };
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + (NP0 + static_cast<size_t>(p.T - 1) * NP) * pb);
+  auto level_off = [&](int k, int slot) -> int { return (k == 0 ? slot : NP0 + (k - 1) * NP + slot) * pe; };
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + static_cast<size_t>(NP0 + (p.T - 1) * NP) * pe * sizeof(TS));
 
-  __shared__ int s_offh[kMaxMask3D], s_offp[kMaxMask3D];
-  __shared__ float s_wt[kMaxMask3D];
   // fp64 residual partials per (level of this pass, warp); each warp adds
   // its own reduced sums in march order, so the partials are deterministic
   __shared__ double s_part[kMax3DSteps][kStencil3DThreads / 32];
@@ -64,11 +64,17 @@ __global__ void __launch_bounds__(kStencil3DThreads)
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   constexpr int kWarps = kStencil3DThreads / 32;
-  for (int i = tid; i < kMax3DSteps * (kStencil3DThreads / 32); i += kStencil3DThreads) (&s_part[0][0])[i] = 0.0;
-  if (tid < p.nm) {
-    s_offh[tid] = p.off_h[tid];
-    s_offp[tid] = p.off_plane[tid];
-    s_wt[tid] = p.wt[tid];
+  constexpr int kM = NM > 0 ? NM : kMaxMask3D;
+  for (int i = tid; i < kMax3DSteps * kWarps; i += kStencil3DThreads) (&s_part[0][0])[i] = 0.0;
+  // mask entries in registers: weights, plane offsets dh, in-plane offsets
+  float wt[kM];
+  int offh[kM], offp[kM];
+  const int nm = NM > 0 ? NM : p.nm;
+#pragma unroll
+  for (int n = 0; n < kM; ++n) {
+    wt[n] = n < nm ? p.wt[n] : 0.0f;
+    offh[n] = n < nm ? p.off_h[n] : 0;
+    offp[n] = n < nm ? p.off_plane[n] : 0;
   }
   if (kTma && tid == 0) {
     mbar_init(bar, 1);
@@ -76,7 +82,6 @@ __global__ void __launch_bounds__(kStencil3DThreads)
     prefetch_tensormap(&map_src);
   }
   __syncthreads();
-  (void)lvl0;
 
   const TS halo = S::store(p.halo);
   const TS* src = static_cast<const TS*>(p.src);
@@ -85,6 +90,8 @@ __global__ void __launch_bounds__(kStencil3DThreads)
   const int ntiles = ncols * p.hchunks;
   const int steps = p.steps;
   uint32_t phase = 0;
+  auto wrap = [](int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); };  // |x| < 2n
+  auto modn = [](int x, int n) { const int r = x % n; return r < 0 ? r + n : r; };
 
   // Work items: a (w, d) tile column over a chunk [h0, h1) of output planes.
   // The march starts steps * R planes early to warm the level rings up.
@@ -103,42 +110,46 @@ __global__ void __launch_bounds__(kStencil3DThreads)
 
     // planes before the grid read the halo value at every level
     for (int k = 0; k < steps; ++k)
-      for (int q = -R; q < 0; ++q) fill_plane(level_plane(k, q), plane_elems, halo);
+      for (int q = -R; q < 0; ++q) {
+        TS* pl = sm + level_off(k, modn(q, k == 0 ? NP0 : NP));
+        for (int e = tid; e < plane_elems; e += kStencil3DThreads) pl[e] = halo;
+      }
     __syncthreads();
 
     auto issue = [&](int plane) {
       fence_proxy_async();
       mbar_arrive_expect_tx(bar, static_cast<uint32_t>(plane_elems * sizeof(TS)));
-      tma_load_3d(level_plane(0, plane), &map_src, gd0, gw0, plane, bar);
+      tma_load_3d(sm + level_off(0, modn(plane, NP0)), &map_src, gd0, gw0, plane, bar);
     };
     if (kTma && tid == 0 && first < p.H) issue(first);
 
-    for (int i = first; i <= last; ++i) {
+    int s0 = modn(first, NP0);  // level-0 slot of plane i
+    int sN = modn(first, NP);   // plane i modulo NP (levels >= 1)
+    for (int i = first; i <= last; ++i, s0 = (s0 + 1 == NP0 ? 0 : s0 + 1), sN = (sN + 1 == NP ? 0 : sN + 1)) {
       // ---- level 0: input plane i
+      TS* pl0 = sm + level_off(0, s0);
       if (i < p.H && !kTma) {
-        TS* pl = level_plane(0, i);
         for (int e = tid; e < plane_elems; e += kStencil3DThreads) {
           const int lw = e / LD, ld = e - lw * LD;
           const int gw = gw0 + lw, gd = gd0 + ld;
-          pl[e] = (gw < 0 || gw >= p.W || gd < 0 || gd >= p.D) ? halo
+          pl0[e] = (gw < 0 || gw >= p.W || gd < 0 || gd >= p.D) ? halo
                                                                 : src[(static_cast<int64_t>(i) * p.W + gw) * p.D + gd];
         }
       } else if (i < p.H) {
         if (!mbar_wait_bounded(bar, phase, p.err)) return;
         phase ^= 1u;
         if (edge && S::load(halo) != 0.0f) {
-          TS* pl = level_plane(0, i);
           for (int e = tid; e < plane_elems; e += kStencil3DThreads) {
             const int lw = e / LD, ld = e - lw * LD;
             const int gw = gw0 + lw, gd = gd0 + ld;
-            if (gw < 0 || gw >= p.W || gd < 0 || gd >= p.D) pl[e] = halo;
+            if (gw < 0 || gw >= p.W || gd < 0 || gd >= p.D) pl0[e] = halo;
           }
         }
       } else {
-        fill_plane(level_plane(0, i), plane_elems, halo);
+        for (int e = tid; e < plane_elems; e += kStencil3DThreads) pl0[e] = halo;
       }
       __syncthreads();
-      // the slot of plane i+1 held plane i-NP-... no longer read: prefetch it
+      // plane i+1's slot held plane i+1-NP0, which no level reads any more
       if (kTma && tid == 0 && i + 1 < p.H && i + 1 <= last) issue(i + 1);
 
       // ---- levels 1..steps
@@ -146,8 +157,12 @@ __global__ void __launch_bounds__(kStencil3DThreads)
         const int q = i - k * R;
         // planes this level must produce for the chunk's output planes
         if (q < max(0, h0 - (steps - k) * R) || q >= h1 + (steps - k) * R) continue;
+        // slot of plane q at level k (q mod NP) and at level k-1
+        const int slot_q = modn(sN - k * R, NP);
+        const int slot_q0 = modn(i - k * R, NP0);  // for level 0 (NP0 slots)
         if (k < steps && q >= p.H) {
-          fill_plane(level_plane(k, q), plane_elems, halo);
+          TS* pl = sm + level_off(k, slot_q);
+          for (int e = tid; e < plane_elems; e += kStencil3DThreads) pl[e] = halo;
           __syncthreads();
           continue;
         }
@@ -155,14 +170,17 @@ __global__ void __launch_bounds__(kStencil3DThreads)
         const int e = R * (steps - k);
         const int w_lo = p.HW - e, w_hi = p.HW + p.TW + e;
         const int d_lo = p.HD - e, d_hi = p.HD + p.TD + e;
-        const TS* nb[NM > 0 ? NM : kMaxMask3D];
-        const int nm = NM > 0 ? NM : p.nm;
+        // neighbour planes q + dh of level k-1, as element offsets
+        int nb[kM];
 #pragma unroll
-        for (int n = 0; n < (NM > 0 ? NM : kMaxMask3D); ++n)
-          if (n < nm) nb[n] = level_plane(k - 1, q + s_offh[n]) + s_offp[n];
-        TS* outp = (k < steps) ? level_plane(k, q) : nullptr;
-        const TS* prevp = level_plane(k - 1, q);
-        // the chunk owns planes [h0, h1): only those count in the residual
+        for (int n = 0; n < kM; ++n) {
+          if (n < nm) {
+            const int sl = (k == 1) ? wrap(slot_q0 + offh[n], NP0) : wrap(slot_q + offh[n], NP);
+            nb[n] = level_off(k - 1, sl) + offp[n];
+          }
+        }
+        const int prev = level_off(k - 1, k == 1 ? slot_q0 : slot_q);
+        const int outo = (k < steps) ? level_off(k, slot_q) : 0;
         const bool report = p.every > 0 && ((p.step0 + k) % p.every) == 0 && q >= h0 && q < h1;
         double acc_res = 0.0;
         for (int lw = w_lo + warp; lw < w_hi; lw += kWarps) {
@@ -174,15 +192,15 @@ __global__ void __launch_bounds__(kStencil3DThreads)
             const int idx = lw * LD + ld;
             TS v;
             if (w_in && gd >= 0 && gd < p.D) {
-              float acc = __fmul_rn(s_wt[0], S::load(nb[0][idx]));
+              float acc = __fmul_rn(wt[0], S::load(sm[nb[0] + idx]));
 #pragma unroll
-              for (int n = 1; n < (NM > 0 ? NM : kMaxMask3D); ++n)
-                if (n < nm) acc = __fadd_rn(acc, __fmul_rn(s_wt[n], S::load(nb[n][idx])));
+              for (int n = 1; n < kM; ++n)
+                if (n < nm) acc = __fadd_rn(acc, __fmul_rn(wt[n], S::load(sm[nb[n] + idx])));
               v = S::store(acc);
               const bool core = w_core && ld >= p.HD && ld < p.HD + p.TD;
               if (core) {
                 if (report) {
-                  const double dlt = static_cast<double>(S::load(v)) - static_cast<double>(S::load(prevp[idx]));
+                  const double dlt = static_cast<double>(S::load(v)) - static_cast<double>(S::load(sm[prev + idx]));
                   acc_res += dlt * dlt;
                 }
                 if (k == steps) dst[(static_cast<int64_t>(q) * p.W + gw) * p.D + gd] = v;
@@ -190,7 +208,7 @@ __global__ void __launch_bounds__(kStencil3DThreads)
             } else {
               v = halo;
             }
-            if (k < steps) outp[idx] = v;
+            if (k < steps) sm[outo + idx] = v;
           }
         }
         if (report) {

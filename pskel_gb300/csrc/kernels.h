@@ -98,6 +98,7 @@ cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const 
 constexpr int kMaxMask3D = 32;
 constexpr int kMax3DSteps = 8;  // time steps fused per pass
 constexpr int kStencil3DThreads = 256;
+constexpr int kPrefetch3D = 3;  // input planes in flight ahead of the march
 
 struct Stencil3DParams {
   int W, H, D;        // h slowest, d fastest

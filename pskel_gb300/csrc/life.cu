@@ -211,8 +211,11 @@ __global__ void __launch_bounds__(kLifeThreads, 3)
       for (int c = 0; c < nchunks; ++c) {
         uint8_t* slot = slots + c_slot * kChunkRows * kLifeLW;
         if (kTma) {
-          if (!mbar_wait_bounded(&bars[c_slot], phase[c_slot], err)) return;
+          // one thread waits; the block barrier publishes the chunk
+          int ok = 1;
+          if (tid == 0) ok = mbar_wait_bounded(&bars[c_slot], phase[c_slot], err) ? 1 : 0;
           phase[c_slot] ^= 1u;
+          if (!__syncthreads_and(ok)) return;
         } else {
           const uint8_t* from = (k == 0) ? src : dst;
           for (int i = tid; i < kChunkRows * 16; i += kLifeThreads) {

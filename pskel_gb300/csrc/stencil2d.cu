@@ -164,8 +164,10 @@ __global__ void __launch_bounds__(kStencil2DThreads)
           tma_load_2d(bufV, &map_v, gx0, gy0, bar);
         }
       }
-      if (!mbar_wait_bounded(bar, phase, p.err)) return;
+      int ok = 1;
+      if (tid == 0) ok = mbar_wait_bounded(bar, phase, p.err) ? 1 : 0;
       phase ^= 1u;
+      if (!__syncthreads_and(ok)) return;
     } else {
       coop_load(bufA, src, gy0, gx0, LW, LH, p.W, p.H, p.pitch);
       if (stage_dst) coop_load(bufB, static_cast<const TS*>(p.dst), gy0, gx0, LW, LH, p.W, p.H, p.pitch);

@@ -163,11 +163,9 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     mbar_arrive_expect_tx(&bars[b], kTileBytes);
     tma_load_2d(buf(b), m, gx0, gy0, &bars[b]);
   };
-  auto wait = [&](int b) -> bool {
-    const bool ok = mbar_wait_bounded(&bars[b], (phase_bits >> b) & 1u, p.err);
-    phase_bits ^= (1u << b);
-    return ok;
-  };
+  // one thread waits on a buffer's barrier; the block barrier that follows
+  // publishes the tile to the other threads
+  auto wait1 = [&](int b) -> bool { return mbar_wait_bounded(&bars[b], (phase_bits >> b) & 1u, p.err); };
 
   if (tid == 0 && static_cast<int>(blockIdx.x) < ntiles) {
     int gy0, gx0;
@@ -191,8 +189,11 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
         load(bn, &map_src, ny0, nx0);
       }
     }
-    if (!wait(bs)) return;
-    if (stage_dst && !wait(bp)) return;
+    int ok = 1;
+    if (tid == 0) ok = (wait1(bs) && (!stage_dst || wait1(bp))) ? 1 : 0;
+    phase_bits ^= (1u << bs);
+    if (stage_dst) phase_bits ^= (1u << bp);
+    if (!__syncthreads_and(ok)) return;
 
     const int gxv = gx0 + x0;
     for (int s = 1; s <= p.steps; ++s) {

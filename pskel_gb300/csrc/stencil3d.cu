@@ -51,11 +51,12 @@ __global__ void __launch_bounds__(kStencil3DThreads)
   const int LW = p.LW, LD = p.LD, NP = p.NP, R = p.R;
   const int plane_elems = LW * LD;
   const int pe = static_cast<int>(plane_bytes<TS>(LW, LD) / sizeof(TS));  // plane stride in elements
-  // level 0 ring has one extra slot so the next plane can load while the
-  // current ones are still read; levels 1..steps-1 have NP slots each
-  const int NP0 = NP + 1;
+  // level 0 ring has kPrefetch3D extra slots: the next planes load while the
+  // current ones are still read; levels 1..steps-1 have NP slots each. Each
+  // level-0 slot has its own mbarrier.
+  const int NP0 = NP + kPrefetch3D;
   auto level_off = [&](int k, int slot) -> int { return (k == 0 ? slot : NP0 + (k - 1) * NP + slot) * pe; };
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + static_cast<size_t>(NP0 + (p.T - 1) * NP) * pe * sizeof(TS));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + static_cast<size_t>(NP0 + (p.T - 1) * NP) * pe * sizeof(TS));
 
   // fp64 residual partials per (level of this pass, warp); each warp adds
   // its own reduced sums in march order, so the partials are deterministic
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(kStencil3DThreads)
     offp[n] = n < nm ? p.off_plane[n] : 0;
   }
   if (kTma && tid == 0) {
-    mbar_init(bar, 1);
+    for (int b = 0; b < NP0; ++b) mbar_init(&bars[b], 1);
     fence_barrier_init();
     prefetch_tensormap(&map_src);
   }
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kStencil3DThreads)
   const int ncols = p.tiles_w * p.tiles_d;
   const int ntiles = ncols * p.hchunks;
   const int steps = p.steps;
-  uint32_t phase = 0;
+  uint32_t phase_bits = 0;  // bit b: parity of the next completion of bars[b]
   auto wrap = [](int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); };  // |x| < 2n
   auto modn = [](int x, int n) { const int r = x % n; return r < 0 ? r + n : r; };
 
@@ -117,11 +118,13 @@ __global__ void __launch_bounds__(kStencil3DThreads)
     __syncthreads();
 
     auto issue = [&](int plane) {
+      const int b = modn(plane, NP0);
       fence_proxy_async();
-      mbar_arrive_expect_tx(bar, static_cast<uint32_t>(plane_elems * sizeof(TS)));
-      tma_load_3d(sm + level_off(0, modn(plane, NP0)), &map_src, gd0, gw0, plane, bar);
+      mbar_arrive_expect_tx(&bars[b], static_cast<uint32_t>(plane_elems * sizeof(TS)));
+      tma_load_3d(sm + level_off(0, b), &map_src, gd0, gw0, plane, &bars[b]);
     };
-    if (kTma && tid == 0 && first < p.H) issue(first);
+    if (kTma && tid == 0)
+      for (int j = first; j < first + kPrefetch3D && j < p.H && j <= last; ++j) issue(j);
 
     int s0 = modn(first, NP0);  // level-0 slot of plane i
     int sN = modn(first, NP);   // plane i modulo NP (levels >= 1)
@@ -136,8 +139,13 @@ __global__ void __launch_bounds__(kStencil3DThreads)
                                                                 : src[(static_cast<int64_t>(i) * p.W + gw) * p.D + gd];
         }
       } else if (i < p.H) {
-        if (!mbar_wait_bounded(bar, phase, p.err)) return;
-        phase ^= 1u;
+        // one thread waits for the plane; the barrier below publishes it
+        int ok = 1;
+        if (tid == 0) {
+          ok = mbar_wait_bounded(&bars[s0], (phase_bits >> s0) & 1u, p.err) ? 1 : 0;
+        }
+        phase_bits ^= (1u << s0);
+        if (!__syncthreads_and(ok)) return;
         if (edge && S::load(halo) != 0.0f) {
           for (int e = tid; e < plane_elems; e += kStencil3DThreads) {
             const int lw = e / LD, ld = e - lw * LD;
@@ -149,8 +157,8 @@ __global__ void __launch_bounds__(kStencil3DThreads)
         for (int e = tid; e < plane_elems; e += kStencil3DThreads) pl0[e] = halo;
       }
       __syncthreads();
-      // plane i+1's slot held plane i+1-NP0, which no level reads any more
-      if (kTma && tid == 0 && i + 1 < p.H && i + 1 <= last) issue(i + 1);
+      // plane i+P's slot held plane i+P-NP0 = i-2R-1, which no level reads any more
+      if (kTma && tid == 0 && i + kPrefetch3D < p.H && i + kPrefetch3D <= last) issue(i + kPrefetch3D);
 
       // ---- levels 1..steps
       for (int k = 1; k <= steps; ++k) {
@@ -272,7 +280,7 @@ cudaError_t launch3d(const CUtensorMap* map, const Stencil3DParams& p, int ctas,
 
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize) {
   const size_t pb = (static_cast<size_t>(LW) * LD * esize + 127) & ~size_t(127);
-  return 128 + (static_cast<size_t>(NP + 1) + static_cast<size_t>(T - 1) * NP) * pb + 16;
+  return (static_cast<size_t>(NP + kPrefetch3D) + static_cast<size_t>(T - 1) * NP) * pb + 8 * (NP + kPrefetch3D);
 }
 
 int stencil3d_max_ctas_per_sm(size_t smem) {

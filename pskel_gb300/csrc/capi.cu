@@ -540,15 +540,73 @@ pskel_status validate3d(const pskel_stencil* st, const void* in, const void* out
   return PSKEL_OK;
 }
 
+// One step per launch with the streaming kernel (no temporal blocking).
+static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
+                             int64_t iters, int R, const pskel_schedule* sched, int64_t every, double* residuals,
+                             double* partials_override, int64_t partials_cap, DeviceContext* c, cudaStream_t s) {
+  Stencil3DParams p;
+  memset(&p, 0, sizeof(p));
+  p.W = static_cast<int>(W);
+  p.H = static_cast<int>(H);
+  p.D = static_cast<int>(D);
+  p.R = R;
+  p.nm = st.mask.size;
+  for (int n = 0; n < p.nm; ++n) {
+    p.off_h[n] = st.mask.offsets[3 * n];
+    p.off_w[n] = st.mask.offsets[3 * n + 1];
+    p.off_d[n] = st.mask.offsets[3 * n + 2];
+    p.wt[n] = st.mask.weights[n];
+  }
+  p.halo = st.mask.halo_value;
+  p.err = c->err;
+  p.every = static_cast<int>(every);
+  p.residuals = residuals;
+  const size_t esz = dtype_size(st.dtype);
+  const bool cross7 = stream3d_is_cross7(st.mask.offsets, st.mask.size, D) &&
+                      (reinterpret_cast<uintptr_t>(in) % (4 * esz)) == 0 &&
+                      (reinterpret_cast<uintptr_t>(out) % (4 * esz)) == 0;
+  // h chunks: a few blocks per SM slot, each marching at least 16 planes
+  const int64_t cols = (cross7 ? (D + 127) / 128 : (D + 31) / 32) * ((W + 7) / 8);
+  int64_t chunks = std::max<int64_t>(1, (static_cast<int64_t>(32) * c->sms + cols - 1) / cols);
+  chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / 16));
+  if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
+  p.HC = static_cast<int>((H + chunks - 1) / chunks);
+  p.hchunks = static_cast<int>((H + p.HC - 1) / p.HC);
+  if (every > 0) {
+    const int64_t need = stream3d_ctas(p.W, p.D, p.hchunks, cross7);
+    if (partials_override) {
+      if (need > partials_cap)
+        return fail(PSKEL_ERR_UNSUPPORTED, "residual scratch of %lld partials exceeds the fixed capacity %lld",
+                    (long long)need, (long long)partials_cap);
+      p.partials = partials_override;
+    } else {
+      if (pskel_status q = ensure_buffer(c->partials, static_cast<size_t>(need) * sizeof(double))) return q;
+      p.partials = static_cast<double*>(c->partials.ptr);
+    }
+  }
+  for (int64_t k = 0; k < iters; ++k) {
+    const bool fwd = (k % 2 == 0);
+    p.src = fwd ? in : out;
+    p.dst = fwd ? out : in;
+    p.steps = 1;
+    p.step0 = k;
+    cudaError_t e = stream3d_step(static_cast<int>(st.dtype), p, cross7, s);
+    if (e != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
+  }
+  return PSKEL_OK;
+}
+
 pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
                               int64_t iters, int R, const pskel_schedule* sched, int64_t every, double* residuals,
                               double* partials_override, int64_t partials_cap, DeviceContext* c, cudaStream_t s) {
   const int dtype = static_cast<int>(st.dtype);
   const size_t esz = dtype_size(st.dtype);
   const int vec = static_cast<int>(16 / esz);
-  int T = (sched && sched->time_steps > 0) ? sched->time_steps : 2;
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : 1;
   T = static_cast<int>(std::min<int64_t>(std::min(T, kMax3DSteps), std::max<int64_t>(iters, 1)));
   if (R == 0) T = 1;
+  if (T == 1) return stream3d(st, in, out, W, H, D, iters, R, sched, every, residuals, partials_override,
+                              partials_cap, c, s);
   int TW = (sched && sched->tile_w > 0) ? sched->tile_w : 32;
   int TD = (sched && sched->tile_d > 0) ? sched->tile_d : 64;
   TD = std::max(vec, (TD / vec) * vec);
@@ -597,6 +655,8 @@ pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, 
   p.nm = st.mask.size;
   for (int n = 0; n < p.nm; ++n) {
     p.off_h[n] = st.mask.offsets[3 * n];
+    p.off_w[n] = st.mask.offsets[3 * n + 1];
+    p.off_d[n] = st.mask.offsets[3 * n + 2];
     p.off_plane[n] = st.mask.offsets[3 * n + 1] * LD + st.mask.offsets[3 * n + 2];
     p.wt[n] = st.mask.weights[n];
   }

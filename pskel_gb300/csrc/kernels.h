@@ -113,6 +113,8 @@ struct Stencil3DParams {
   int nm;
   int off_h[kMaxMask3D];      // dh per entry
   int off_plane[kMaxMask3D];  // dw * LD + dd per entry
+  int off_w[kMaxMask3D];      // dw per entry
+  int off_d[kMaxMask3D];      // dd per entry
   float wt[kMaxMask3D];
   float halo;
   const void* src;
@@ -126,6 +128,14 @@ struct Stencil3DParams {
 
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize);
 int stencil3d_max_ctas_per_sm(size_t smem);
+// One step of the streaming (not temporally blocked) kernel: a block per
+// 32 (d) x 8 (w) columns and h chunk of p.HC planes; residual partials, when
+// the step is reported, go to p.partials[one per block].
+// cross7: the 7-point cross in (centre, h-1, h+1, w-1, w+1, d-1, d+1) order
+// with D % 4 == 0 takes the vectorised variant (a block per 128 d x 8 w).
+bool stream3d_is_cross7(const int* offsets, int n, int64_t D);
+int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7);
+cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, bool cross7, cudaStream_t s);
 cudaError_t stencil3d_pass(int dtype, bool use_tma, const CUtensorMap* map_src, const Stencil3DParams& p, int ctas,
                            cudaStream_t s);
 

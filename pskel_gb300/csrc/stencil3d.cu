@@ -241,6 +241,222 @@ __global__ void __launch_bounds__(kStencil3DThreads)
   }
 }
 
+// One step without temporal blocking: each thread owns a (w, d) column of a
+// 32 x 8 block and marches along a chunk of h, reading its neighbours through
+// the read-only cache (the three planes a block touches stay in L1), so every
+// cell is read from DRAM about once and written once. Lanes run along d, the
+// contiguous axis, so every load and store of a warp is one 128-byte line.
+template <class TS, int NM>
+__global__ void __launch_bounds__(256)
+    stream3d_kernel(const __grid_constant__ Stencil3DParams p) {
+  using S = Storage<TS>;
+  constexpr int kM = NM > 0 ? NM : kMaxMask3D;
+  __shared__ double s_part[8];
+  const int nm = NM > 0 ? NM : p.nm;
+  float wt[kM];
+  int oh[kM], ow[kM], od[kM];
+  int64_t off[kM];
+  const int64_t plane = static_cast<int64_t>(p.W) * p.D;
+#pragma unroll
+  for (int n = 0; n < kM; ++n) {
+    wt[n] = n < nm ? p.wt[n] : 0.0f;
+    oh[n] = n < nm ? p.off_h[n] : 0;
+    ow[n] = n < nm ? p.off_w[n] : 0;
+    od[n] = n < nm ? p.off_d[n] : 0;
+    off[n] = oh[n] * plane + static_cast<int64_t>(ow[n]) * p.D + od[n];
+  }
+  const TS* __restrict__ src = static_cast<const TS*>(p.src);
+  TS* __restrict__ dst = static_cast<TS*>(p.dst);
+  const float halo = p.halo;
+  const int d = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int w = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int h0 = blockIdx.z * p.HC;
+  const int h1 = min(p.H, h0 + p.HC);
+  const bool col_ok = d < p.D && w < p.W;
+  // columns whose every neighbour column is inside the grid skip the checks
+  const bool col_inner = col_ok && d >= p.R && d + p.R < p.D && w >= p.R && w + p.R < p.W;
+  const bool report = p.every > 0 && ((p.step0 + 1) % p.every) == 0;
+  double acc_res = 0.0;
+  if (col_ok) {
+    for (int h = h0; h < h1; ++h) {
+      const int64_t c = h * plane + static_cast<int64_t>(w) * p.D + d;
+      float acc;
+      if (col_inner && h >= p.R && h + p.R < p.H) {
+        acc = __fmul_rn(wt[0], S::load(__ldg(src + c + off[0])));
+#pragma unroll
+        for (int n = 1; n < kM; ++n)
+          if (n < nm) acc = __fadd_rn(acc, __fmul_rn(wt[n], S::load(__ldg(src + c + off[n]))));
+      } else {
+        acc = 0.0f;
+#pragma unroll
+        for (int n = 0; n < kM; ++n) {
+          if (n < nm) {
+            const unsigned hh = static_cast<unsigned>(h + oh[n]), ww = static_cast<unsigned>(w + ow[n]);
+            const unsigned dd = static_cast<unsigned>(d + od[n]);
+            const bool in = hh < static_cast<unsigned>(p.H) && ww < static_cast<unsigned>(p.W) &&
+                            dd < static_cast<unsigned>(p.D);
+            const float v = in ? S::load(__ldg(src + c + off[n])) : halo;
+            const float t = __fmul_rn(wt[n], v);
+            acc = (n == 0) ? t : __fadd_rn(acc, t);
+          }
+        }
+      }
+      const TS out = S::store(acc);
+      dst[c] = out;
+      if (report) {
+        const double dl = static_cast<double>(S::load(out)) - static_cast<double>(S::load(__ldg(src + c)));
+        acc_res += dl * dl;
+      }
+    }
+  }
+  if (p.every > 0) {
+    // deterministic: fixed shuffle tree per warp, warps added in order
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc_res += __shfl_down_sync(0xFFFFFFFFu, acc_res, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc_res;
+    __syncthreads();
+    if (threadIdx.x == 0 && report) {
+      double t = 0.0;
+      for (int i = 0; i < 8; ++i) t += s_part[i];
+      const int cta = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+      p.partials[cta] = t;
+    }
+  }
+}
+
+// The 7-point cross (centre, h-1, h+1, w-1, w+1, d-1, d+1, summed in that
+// order) without temporal blocking, vectorised: each thread owns 4
+// consecutive d cells of one w row and marches along h keeping the planes
+// h-1, h, h+1 of its cells in registers; it loads per plane one vector of
+// plane h+1 and the two w-neighbour vectors, and gets the d-1 / d+4
+// neighbours from the adjacent lanes (the warp's edge lanes load them).
+// Requires D % 4 == 0.
+template <class TS>
+__device__ __forceinline__ void ldv4(const TS* p, float* r) {
+  if constexpr (sizeof(TS) == 4) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    r[0] = v.x;
+    r[1] = v.y;
+    r[2] = v.z;
+    r[3] = v.w;
+  } else {
+    const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+    r[0] = __uint_as_float(v.x << 16);
+    r[1] = __uint_as_float(v.x & 0xFFFF0000u);
+    r[2] = __uint_as_float(v.y << 16);
+    r[3] = __uint_as_float(v.y & 0xFFFF0000u);
+  }
+}
+template <class TS>
+__device__ __forceinline__ void stv4(TS* p, const float* r) {
+  if constexpr (sizeof(TS) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
+  } else {
+    const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(r[0]));
+    const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(r[1]));
+    const uint32_t c = __bfloat16_as_ushort(__float2bfloat16_rn(r[2]));
+    const uint32_t d = __bfloat16_as_ushort(__float2bfloat16_rn(r[3]));
+    *reinterpret_cast<uint2*>(p) = make_uint2(a | (b << 16), c | (d << 16));
+  }
+}
+
+template <class TS>
+__global__ void __launch_bounds__(256) stream3d_cross7_kernel(const __grid_constant__ Stencil3DParams p) {
+  using S = Storage<TS>;
+  __shared__ double s_part[8];
+  float wt[7];
+#pragma unroll
+  for (int n = 0; n < 7; ++n) wt[n] = p.wt[n];
+  const TS* __restrict__ src = static_cast<const TS*>(p.src);
+  TS* __restrict__ dst = static_cast<TS*>(p.dst);
+  const float halo = p.halo;
+  const int lane = threadIdx.x & 31;
+  const int d = (blockIdx.x * 32 + lane) * 4;
+  const int w = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int h0 = blockIdx.z * p.HC;
+  const int h1 = min(p.H, h0 + p.HC);
+  const bool col_ok = d < p.D && w < p.W;
+  const int64_t plane = static_cast<int64_t>(p.W) * p.D;
+  const bool report = p.every > 0 && ((p.step0 + 1) % p.every) == 0;
+  double acc_res = 0.0;
+  float dn[4], cur[4], up[4];
+  const int64_t col = static_cast<int64_t>(w) * p.D + d;
+  auto load_plane = [&](int h, float* r) {
+    if (col_ok && h >= 0 && h < p.H) {
+      ldv4(src + h * plane + col, r);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) r[c] = halo;
+    }
+  };
+  load_plane(h0 - 1, dn);
+  load_plane(h0, cur);
+  for (int h = h0; h < h1; ++h) {
+    load_plane(h + 1, up);
+    float wm[4], wp[4];
+    if (col_ok && w > 0) {
+      ldv4(src + h * plane + col - p.D, wm);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) wm[c] = halo;
+    }
+    if (col_ok && w + 1 < p.W) {
+      ldv4(src + h * plane + col + p.D, wp);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) wp[c] = halo;
+    }
+    // d-1 of element 0 and d+4 of element 3: from the neighbouring lanes,
+    // edge lanes read them (or the halo value beyond the grid)
+    float dl = __shfl_up_sync(0xFFFFFFFFu, cur[3], 1);
+    float dr = __shfl_down_sync(0xFFFFFFFFu, cur[0], 1);
+    if (lane == 0) dl = (col_ok && d > 0) ? S::load(src[h * plane + col - 1]) : halo;
+    if (lane == 31 || d + 4 >= p.D) dr = (col_ok && d + 4 < p.D) ? S::load(src[h * plane + col + 4]) : halo;
+    if (col_ok) {
+      float res[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float l = (c == 0) ? dl : cur[c - 1];
+        const float r = (c == 3) ? dr : cur[c + 1];
+        float acc = __fmul_rn(wt[0], cur[c]);
+        acc = __fadd_rn(acc, __fmul_rn(wt[1], dn[c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[2], up[c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[3], wm[c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[4], wp[c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[5], l));
+        acc = __fadd_rn(acc, __fmul_rn(wt[6], r));
+        res[c] = acc;
+      }
+      stv4(dst + h * plane + col, res);
+      if (report) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const float stored = S::load(S::store(res[c]));
+          const double dl2 = static_cast<double>(stored) - static_cast<double>(cur[c]);
+          acc_res += dl2 * dl2;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      dn[c] = cur[c];
+      cur[c] = up[c];
+    }
+  }
+  if (p.every > 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc_res += __shfl_down_sync(0xFFFFFFFFu, acc_res, o);
+    if (lane == 0) s_part[threadIdx.x >> 5] = acc_res;
+    __syncthreads();
+    if (threadIdx.x == 0 && report) {
+      double t = 0.0;
+      for (int i = 0; i < 8; ++i) t += s_part[i];
+      const int cta = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+      p.partials[cta] = t;
+    }
+  }
+}
+
 // Sums the per-CTA partials of each reported step in CTA order and stores
 // the square root at residuals[slot0 + j].
 __global__ void reduce3d_residual(const double* __restrict__ partials, int nctas, int steps, int64_t step0, int every,
@@ -276,7 +492,40 @@ cudaError_t launch3d(const CUtensorMap* map, const Stencil3DParams& p, int ctas,
   return cudaGetLastError();
 }
 
+template <class TS, int NM>
+cudaError_t launch_stream(const Stencil3DParams& p, bool cross7, cudaStream_t s) {
+  const dim3 grid(cross7 ? (p.D + 127) / 128 : (p.D + 31) / 32, (p.W + 7) / 8, p.hchunks);
+  if (cross7)
+    stream3d_cross7_kernel<TS><<<grid, 256, 0, s>>>(p);
+  else
+    stream3d_kernel<TS, NM><<<grid, 256, 0, s>>>(p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || p.every <= 0 || ((p.step0 + 1) % p.every) != 0) return e;
+  const int nctas = static_cast<int>(grid.x * grid.y * grid.z);
+  reduce3d_residual<<<1, 256, 0, s>>>(p.partials, nctas, 1, p.step0, p.every, p.residuals);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+bool stream3d_is_cross7(const int* offsets, int n, int64_t D) {
+  static const int k[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+  if (n != 7 || D % 4 != 0) return false;
+  for (int i = 0; i < 7; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (offsets[3 * i + j] != k[i][j]) return false;
+  return true;
+}
+
+int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7) {
+  return static_cast<int64_t>(cross7 ? (D + 127) / 128 : (D + 31) / 32) * ((W + 7) / 8) * hchunks;
+}
+
+cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, bool cross7, cudaStream_t s) {
+  if (dtype == 2)
+    return p.nm == 7 ? launch_stream<__nv_bfloat16, 7>(p, cross7, s) : launch_stream<__nv_bfloat16, 0>(p, cross7, s);
+  return p.nm == 7 ? launch_stream<float, 7>(p, cross7, s) : launch_stream<float, 0>(p, cross7, s);
+}
 
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize) {
   const size_t pb = (static_cast<size_t>(LW) * LD * esize + 127) & ~size_t(127);

@@ -112,8 +112,11 @@ def test_heat3d_c4_size_vs_oracle_and_fp64_error(cuda, oracle_mod):
     r2, n2 = run3d(cuda, heat(keep), a, b, 50, every=10, sched=dict(time_steps=2, tile_w=0, tile_h=0, tile_d=0, ctas=0))
     r3, n3 = run3d(cuda, heat(keep), a, b, 50, every=10, sched=dict(time_steps=3, tile_w=16, tile_h=0, tile_d=32,
                                                                      ctas=0))
+    r1, n1 = run3d(cuda, heat(keep), a, b, 50, every=10)  # default: one step per launch, streaming kernel
     assert np.array_equal(bits(r2), bits(r3))
+    assert np.array_equal(bits(r1), bits(r2))
     np.testing.assert_allclose(n2, n3, rtol=RES_RTOL, atol=0)
+    np.testing.assert_allclose(n1, n2, rtol=RES_RTOL, atol=0)
     assert np.all(np.diff(n2) < 0), "the heat equation's residual must decay"
     c, d = grids(128, 128, 128, 2, "f32")
     g32, _ = run3d(cuda, heat(keep), c, d, 50)

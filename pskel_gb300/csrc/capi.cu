@@ -566,7 +566,7 @@ static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64
                       (reinterpret_cast<uintptr_t>(in) % (4 * esz)) == 0 &&
                       (reinterpret_cast<uintptr_t>(out) % (4 * esz)) == 0;
   // h chunks: a few blocks per SM slot, each marching at least 16 planes
-  const int64_t cols = (cross7 ? (D + 127) / 128 : (D + 31) / 32) * ((W + 7) / 8);
+  const int64_t cols = (cross7 ? (D + 127) / 128 : (D + 31) / 32) * (cross7 ? (W + 15) / 16 : (W + 7) / 8);
   int64_t chunks = std::max<int64_t>(1, (static_cast<int64_t>(32) * c->sms + cols - 1) / cols);
   chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / 16));
   if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);

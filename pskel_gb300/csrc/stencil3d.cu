@@ -372,76 +372,82 @@ __global__ void __launch_bounds__(256) stream3d_cross7_kernel(const __grid_const
   const float halo = p.halo;
   const int lane = threadIdx.x & 31;
   const int d = (blockIdx.x * 32 + lane) * 4;
-  const int w = blockIdx.y * 8 + (threadIdx.x >> 5);
+  // two adjacent w rows per thread: each row's w-neighbour on the inside is
+  // the other row, so a plane costs 4 vector loads for 8 cells
+  const int w = blockIdx.y * 16 + (threadIdx.x >> 5) * 2;
   const int h0 = blockIdx.z * p.HC;
   const int h1 = min(p.H, h0 + p.HC);
-  const bool col_ok = d < p.D && w < p.W;
+  const bool d_ok = d < p.D;
+  const bool row_ok[2] = {d_ok && w < p.W, d_ok && w + 1 < p.W};
   const int64_t plane = static_cast<int64_t>(p.W) * p.D;
   const bool report = p.every > 0 && ((p.step0 + 1) % p.every) == 0;
   double acc_res = 0.0;
-  float dn[4], cur[4], up[4];
+  float dn[2][4], cur[2][4], up[2][4];
   const int64_t col = static_cast<int64_t>(w) * p.D + d;
-  auto load_plane = [&](int h, float* r) {
-    if (col_ok && h >= 0 && h < p.H) {
-      ldv4(src + h * plane + col, r);
+  auto ld_or_halo = [&](bool ok, int64_t at, float* r) {
+    if (ok) {
+      ldv4(src + at, r);
     } else {
 #pragma unroll
       for (int c = 0; c < 4; ++c) r[c] = halo;
     }
   };
-  load_plane(h0 - 1, dn);
-  load_plane(h0, cur);
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    ld_or_halo(row_ok[j] && h0 >= 1, (h0 - 1) * plane + col + j * p.D, dn[j]);
+    ld_or_halo(row_ok[j] && h0 < p.H, h0 * plane + col + j * p.D, cur[j]);
+  }
   for (int h = h0; h < h1; ++h) {
-    load_plane(h + 1, up);
+    const int64_t base = h * plane + col;
     float wm[4], wp[4];
-    if (col_ok && w > 0) {
-      ldv4(src + h * plane + col - p.D, wm);
-    } else {
 #pragma unroll
-      for (int c = 0; c < 4; ++c) wm[c] = halo;
-    }
-    if (col_ok && w + 1 < p.W) {
-      ldv4(src + h * plane + col + p.D, wp);
-    } else {
+    for (int j = 0; j < 2; ++j) ld_or_halo(row_ok[j] && h + 1 < p.H, base + plane + j * p.D, up[j]);
+    ld_or_halo(row_ok[0] && w > 0, base - p.D, wm);
+    ld_or_halo(row_ok[1] && w + 2 < p.W, base + 2 * p.D, wp);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) wp[c] = halo;
-    }
-    // d-1 of element 0 and d+4 of element 3: from the neighbouring lanes,
-    // edge lanes read them (or the halo value beyond the grid)
-    float dl = __shfl_up_sync(0xFFFFFFFFu, cur[3], 1);
-    float dr = __shfl_down_sync(0xFFFFFFFFu, cur[0], 1);
-    if (lane == 0) dl = (col_ok && d > 0) ? S::load(src[h * plane + col - 1]) : halo;
-    if (lane == 31 || d + 4 >= p.D) dr = (col_ok && d + 4 < p.D) ? S::load(src[h * plane + col + 4]) : halo;
-    if (col_ok) {
+    for (int j = 0; j < 2; ++j) {
+      // d-1 of element 0 and d+4 of element 3: from the neighbouring lanes,
+      // edge lanes read them (or the halo value beyond the grid). Every lane
+      // takes part in the shuffles, whether or not its row is inside the grid.
+      float dl = __shfl_up_sync(0xFFFFFFFFu, cur[j][3], 1);
+      float dr = __shfl_down_sync(0xFFFFFFFFu, cur[j][0], 1);
+      if (!row_ok[j]) continue;
+      const float* wmj = (j == 0) ? wm : cur[0];
+      const float* wpj = (j == 0) ? (row_ok[1] ? cur[1] : wp) : wp;
+      const int64_t at = base + j * p.D;
+      if (lane == 0) dl = (d > 0) ? S::load(src[at - 1]) : halo;
+      if (lane == 31 || d + 4 >= p.D) dr = (d + 4 < p.D) ? S::load(src[at + 4]) : halo;
       float res[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const float l = (c == 0) ? dl : cur[c - 1];
-        const float r = (c == 3) ? dr : cur[c + 1];
-        float acc = __fmul_rn(wt[0], cur[c]);
-        acc = __fadd_rn(acc, __fmul_rn(wt[1], dn[c]));
-        acc = __fadd_rn(acc, __fmul_rn(wt[2], up[c]));
-        acc = __fadd_rn(acc, __fmul_rn(wt[3], wm[c]));
-        acc = __fadd_rn(acc, __fmul_rn(wt[4], wp[c]));
+        const float l = (c == 0) ? dl : cur[j][c - 1];
+        const float r = (c == 3) ? dr : cur[j][c + 1];
+        float acc = __fmul_rn(wt[0], cur[j][c]);
+        acc = __fadd_rn(acc, __fmul_rn(wt[1], dn[j][c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[2], up[j][c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[3], wmj[c]));
+        acc = __fadd_rn(acc, __fmul_rn(wt[4], wpj[c]));
         acc = __fadd_rn(acc, __fmul_rn(wt[5], l));
         acc = __fadd_rn(acc, __fmul_rn(wt[6], r));
         res[c] = acc;
       }
-      stv4(dst + h * plane + col, res);
+      stv4(dst + at, res);
       if (report) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const float stored = S::load(S::store(res[c]));
-          const double dl2 = static_cast<double>(stored) - static_cast<double>(cur[c]);
+          const double dl2 = static_cast<double>(stored) - static_cast<double>(cur[j][c]);
           acc_res += dl2 * dl2;
         }
       }
     }
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      dn[c] = cur[c];
-      cur[c] = up[c];
-    }
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        dn[j][c] = cur[j][c];
+        cur[j][c] = up[j][c];
+      }
   }
   if (p.every > 0) {
 #pragma unroll
@@ -494,7 +500,7 @@ cudaError_t launch3d(const CUtensorMap* map, const Stencil3DParams& p, int ctas,
 
 template <class TS, int NM>
 cudaError_t launch_stream(const Stencil3DParams& p, bool cross7, cudaStream_t s) {
-  const dim3 grid(cross7 ? (p.D + 127) / 128 : (p.D + 31) / 32, (p.W + 7) / 8, p.hchunks);
+  const dim3 grid(cross7 ? (p.D + 127) / 128 : (p.D + 31) / 32, cross7 ? (p.W + 15) / 16 : (p.W + 7) / 8, p.hchunks);
   if (cross7)
     stream3d_cross7_kernel<TS><<<grid, 256, 0, s>>>(p);
   else
@@ -518,7 +524,8 @@ bool stream3d_is_cross7(const int* offsets, int n, int64_t D) {
 }
 
 int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7) {
-  return static_cast<int64_t>(cross7 ? (D + 127) / 128 : (D + 31) / 32) * ((W + 7) / 8) * hchunks;
+  return static_cast<int64_t>(cross7 ? (D + 127) / 128 : (D + 31) / 32) * (cross7 ? (W + 15) / 16 : (W + 7) / 8) *
+         hchunks;
 }
 
 cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, bool cross7, cudaStream_t s) {

@@ -1,0 +1,215 @@
+// Device code shared by the register-windowed 2D kernel and the batched
+// persistent kernel: vector helpers, mask shapes and the per-tile routine.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pskel {
+namespace fast2d {
+
+template <class TS>
+struct Vec;
+template <>
+struct Vec<float> {
+  static constexpr int N = 4;
+};
+template <>
+struct Vec<__nv_bfloat16> {
+  static constexpr int N = 4;
+};
+
+__device__ __forceinline__ void ld_vec(const float* p, float* r) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  r[0] = v.x;
+  r[1] = v.y;
+  r[2] = v.z;
+  r[3] = v.w;
+}
+__device__ __forceinline__ void ld_vec(const __nv_bfloat16* p, float* r) {
+  const uint2 v = *reinterpret_cast<const uint2*>(p);
+  r[0] = __uint_as_float(v.x << 16);
+  r[1] = __uint_as_float(v.x & 0xFFFF0000u);
+  r[2] = __uint_as_float(v.y << 16);
+  r[3] = __uint_as_float(v.y & 0xFFFF0000u);
+}
+__device__ __forceinline__ void st_vec(float* p, const float* r) {
+  *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
+}
+__device__ __forceinline__ void st_vec(__nv_bfloat16* p, const float* r) {
+  const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(r[0]));
+  const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(r[1]));
+  const uint32_t c = __bfloat16_as_ushort(__float2bfloat16_rn(r[2]));
+  const uint32_t d = __bfloat16_as_ushort(__float2bfloat16_rn(r[3]));
+  *reinterpret_cast<uint2*>(p) = make_uint2(a | (b << 16), c | (d << 16));
+}
+__device__ __forceinline__ float ld1(const float* p) { return *p; }
+__device__ __forceinline__ float ld1(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+
+// Mask shapes of reach 1, entries in summation order.
+template <int K>
+struct Shape {
+  int n;
+  int dh[9];
+  int dw[9];
+};
+template <int K>
+__host__ __device__ constexpr Shape<K> shape_of() {
+  if constexpr (K == 0) return Shape<0>{4, {-1, 1, 0, 0}, {0, 0, -1, 1}};
+  if constexpr (K == 1) return Shape<1>{5, {0, -1, 1, 0, 0}, {0, 0, 0, -1, 1}};
+  if constexpr (K == 2) return Shape<2>{9, {-1, -1, -1, 0, 0, 0, 1, 1, 1}, {-1, 0, 1, -1, 0, 1, -1, 0, 1}};
+}
+
+constexpr int kFastThreads = 512;
+constexpr int kFastBufs = 3;  // rotating tile buffers: source, partner, next source
+
+// Wind vector at (gy, gx..gx+3) straight from global memory (read-only path;
+// the tile's winds stay in L1 across the steps of a pass). Zero outside the grid.
+template <class TS>
+__device__ __forceinline__ void ld_wind(const TS* f, int64_t pitch, int gy, int gx, int W, int H, float* r) {
+  if (gy >= 0 && gy < H && gx >= 0 && gx + 4 <= W) {
+    const TS* q = f + static_cast<int64_t>(gy) * pitch + gx;
+    if constexpr (sizeof(TS) == 4) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(q));
+      r[0] = v.x;
+      r[1] = v.y;
+      r[2] = v.z;
+      r[3] = v.w;
+    } else {
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(q));
+      r[0] = __uint_as_float(v.x << 16);
+      r[1] = __uint_as_float(v.x & 0xFFFF0000u);
+      r[2] = __uint_as_float(v.y << 16);
+      r[3] = __uint_as_float(v.y & 0xFFFF0000u);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int x = gx + c;
+      r[c] = (gy >= 0 && gy < H && x >= 0 && x < W) ? ld1(f + static_cast<int64_t>(gy) * pitch + x) : 0.0f;
+    }
+  }
+}
+
+// Geometry and op parameters of one tile's grid (passed in registers).
+struct TileGeom {
+  int W, H, ring, steps;
+  int TW, TH, HX, HY;
+  int64_t pitch;
+  float K, dt, inv_dx;
+  const void* u;
+  const void* v;
+};
+
+// Runs g.steps steps on a staged tile (source tile in sbuf, the partner
+// buffer pbuf holding the destination's ring when the tile touches it), then
+// writes the core's interior cells to dst. All threads of the block call it.
+template <class TS, int OpK, int S>
+__device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, const TileGeom& g, int gy0, int gx0,
+                                                bool ring_tile, const float* wt) {
+  constexpr int N = Vec<TS>::N;
+  constexpr int LW = 32 * N;
+  constexpr bool kAdvect = (OpK == 3);
+  constexpr auto shp = shape_of<(OpK < 3 ? OpK : 0)>();
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int x0 = lane * N;
+  const int yb = 1 + warp * S;
+  const TS* wu = static_cast<const TS*>(g.u);
+  const TS* wv = static_cast<const TS*>(g.v);
+  const int gxv = gx0 + x0;
+  for (int s = 1; s <= g.steps; ++s) {
+    const TS* in = ((s & 1) ? sbuf : pbuf);
+    TS* out = ((s & 1) ? pbuf : sbuf);
+    // window: rows yb-1 .. yb+S, each [left, v0..v3, right]; the left and
+    // right neighbours come from the adjacent lanes (one warp spans a row)
+    float win[S + 2][N + 2];
+#pragma unroll
+    for (int k = 0; k < S + 2; ++k) {
+      ld_vec(in + (yb - 1 + k) * LW + x0, &win[k][1]);
+      win[k][0] = __shfl_up_sync(0xFFFFFFFFu, win[k][N], 1);
+      win[k][N + 1] = __shfl_down_sync(0xFFFFFFFFu, win[k][1], 1);
+    }
+#pragma unroll
+    for (int k = 1; k <= S; ++k) {
+      const int y = yb - 1 + k;
+      float res[N];
+      if constexpr (!kAdvect) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          float acc = __fmul_rn(wt[0], win[k + shp.dh[0]][1 + c + shp.dw[0]]);
+#pragma unroll
+          for (int n = 1; n < shp.n; ++n) acc = __fadd_rn(acc, __fmul_rn(wt[n], win[k + shp.dh[n]][1 + c + shp.dw[n]]));
+          res[c] = acc;
+        }
+      } else {
+        float uu[N], vv[N];
+        ld_wind(wu, g.pitch, gy0 + y, gxv, g.W, g.H, uu);
+        ld_wind(wv, g.pitch, gy0 + y, gxv, g.W, g.H, vv);
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          const float cc = win[k][1 + c];
+          const float n_ = win[k - 1][1 + c];
+          const float e_ = win[k][2 + c];
+          const float w_ = win[k][c];
+          const float s_ = win[k + 1][1 + c];
+          const float sum = __fsub_rn(__fmul_rn(4.0f, cc), __fadd_rn(__fadd_rn(__fadd_rn(n_, e_), w_), s_));
+          const float xw = uu[c], yw = vv[c];
+          const float cvy = (yw > 0.0f) ? yw : -yw;  // yf * yw with yf = +-1
+          const float cvx = (xw > 0.0f) ? xw : -xw;
+          const float nbx = (xw > 0.0f) ? e_ : w_;
+          const float nby = (yw > 0.0f) ? s_ : n_;
+          const float temp_wind = __fsub_rn(__fmul_rn(-cvx, __fmul_rn(__fsub_rn(cc, nbx), g.inv_dx)),
+                                            __fmul_rn(cvy, __fmul_rn(__fsub_rn(cc, nby), g.inv_dx)));
+          const float cond = __fmul_rn(__fmul_rn(-g.K, __fmul_rn(sum, 0.25f)), g.dt);
+          res[c] = __fadd_rn(__fadd_rn(cc, cond), __fmul_rn(temp_wind, g.dt));
+        }
+      }
+      TS* o = out + y * LW + x0;
+      if (ring_tile) {
+        // cells outside r <= h < H-r, r <= w < W-r keep this buffer's value
+        const int gy = gy0 + y;
+        const bool row_in = gy >= g.ring && gy < g.H - g.ring;
+        float old[N];
+        ld_vec(o, old);
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          const int gx = gxv + c;
+          if (!(row_in && gx >= g.ring && gx < g.W - g.ring)) res[c] = old[c];
+        }
+      }
+      st_vec(o, res);
+    }
+    __syncthreads();
+  }
+
+  // core -> global, interior cells only, vector stores
+  const TS* fin = ((g.steps & 1) ? pbuf : sbuf);
+  const int vpr = g.TW / N;
+  for (int i = tid; i < g.TH * vpr; i += kFastThreads) {
+    const int r = i / vpr;
+    const int cv = i - r * vpr;
+    const int y = g.HY + r, x = g.HX + cv * N;
+    const int gy = gy0 + y, gx = gx0 + x;
+    if (gy < g.ring || gy >= g.H - g.ring) continue;
+    if (gx + N <= g.ring || gx >= g.W - g.ring) continue;
+    TS* d = dst + static_cast<int64_t>(gy) * g.pitch + gx;
+    const TS* sp = fin + y * LW + x;
+    constexpr int kVecBytes = N * static_cast<int>(sizeof(TS));
+    if (gx >= g.ring && gx + N <= g.W - g.ring && (reinterpret_cast<uintptr_t>(d) & (kVecBytes - 1)) == 0) {
+      if constexpr (kVecBytes == 16)
+        *reinterpret_cast<uint4*>(d) = *reinterpret_cast<const uint4*>(sp);
+      else
+        *reinterpret_cast<uint2*>(d) = *reinterpret_cast<const uint2*>(sp);
+    } else {
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const int xx = gx + k;
+        if (xx >= g.ring && xx < g.W - g.ring) d[k] = sp[k];
+      }
+    }
+  }
+}
+
+}  // namespace fast2d
+}  // namespace pskel

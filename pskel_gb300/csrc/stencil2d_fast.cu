@@ -16,96 +16,14 @@
 //
 // Arithmetic is the oracle's: products and sums in mask order with
 // __fmul_rn/__fadd_rn (no contraction), bf16 results rounded every step.
-#include "common.cuh"
-#include "kernels.h"
+#include "fast2d_tile.cuh"
 
 namespace pskel {
 namespace {
 
-template <class TS>
-struct Vec;
-template <>
-struct Vec<float> {
-  static constexpr int N = 4;
-};
-template <>
-struct Vec<__nv_bfloat16> {
-  static constexpr int N = 4;
-};
-
-__device__ __forceinline__ void ld_vec(const float* p, float* r) {
-  const float4 v = *reinterpret_cast<const float4*>(p);
-  r[0] = v.x;
-  r[1] = v.y;
-  r[2] = v.z;
-  r[3] = v.w;
-}
-__device__ __forceinline__ void ld_vec(const __nv_bfloat16* p, float* r) {
-  const uint2 v = *reinterpret_cast<const uint2*>(p);
-  r[0] = __uint_as_float(v.x << 16);
-  r[1] = __uint_as_float(v.x & 0xFFFF0000u);
-  r[2] = __uint_as_float(v.y << 16);
-  r[3] = __uint_as_float(v.y & 0xFFFF0000u);
-}
-__device__ __forceinline__ void st_vec(float* p, const float* r) {
-  *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
-}
-__device__ __forceinline__ void st_vec(__nv_bfloat16* p, const float* r) {
-  const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(r[0]));
-  const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(r[1]));
-  const uint32_t c = __bfloat16_as_ushort(__float2bfloat16_rn(r[2]));
-  const uint32_t d = __bfloat16_as_ushort(__float2bfloat16_rn(r[3]));
-  *reinterpret_cast<uint2*>(p) = make_uint2(a | (b << 16), c | (d << 16));
-}
-__device__ __forceinline__ float ld1(const float* p) { return *p; }
-__device__ __forceinline__ float ld1(const __nv_bfloat16* p) { return __bfloat162float(*p); }
-
-// Mask shapes of reach 1, entries in summation order.
-template <int K>
-struct Shape {
-  int n;
-  int dh[9];
-  int dw[9];
-};
-template <int K>
-__host__ __device__ constexpr Shape<K> shape_of() {
-  if constexpr (K == 0) return Shape<0>{4, {-1, 1, 0, 0}, {0, 0, -1, 1}};
-  if constexpr (K == 1) return Shape<1>{5, {0, -1, 1, 0, 0}, {0, 0, 0, -1, 1}};
-  if constexpr (K == 2) return Shape<2>{9, {-1, -1, -1, 0, 0, 0, 1, 1, 1}, {-1, 0, 1, -1, 0, 1, -1, 0, 1}};
-}
+using namespace fast2d;
 
 // OpK: 0..2 linear shapes above, 3 = advection.
-constexpr int kFastThreads = 512;
-constexpr int kFastBufs = 3;  // rotating tile buffers: source, partner, next source
-
-// Wind vector at (gy, gx..gx+3) straight from global memory (read-only path;
-// the tile's winds stay in L1 across the steps of a pass). Zero outside the grid.
-template <class TS>
-__device__ __forceinline__ void ld_wind(const TS* f, int64_t pitch, int gy, int gx, int W, int H, float* r) {
-  if (gy >= 0 && gy < H && gx >= 0 && gx + 4 <= W) {
-    const TS* q = f + static_cast<int64_t>(gy) * pitch + gx;
-    if constexpr (sizeof(TS) == 4) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(q));
-      r[0] = v.x;
-      r[1] = v.y;
-      r[2] = v.z;
-      r[3] = v.w;
-    } else {
-      const uint2 v = __ldg(reinterpret_cast<const uint2*>(q));
-      r[0] = __uint_as_float(v.x << 16);
-      r[1] = __uint_as_float(v.x & 0xFFFF0000u);
-      r[2] = __uint_as_float(v.y << 16);
-      r[3] = __uint_as_float(v.y & 0xFFFF0000u);
-    }
-  } else {
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int x = gx + c;
-      r[c] = (gy >= 0 && gy < H && x >= 0 && x < W) ? ld1(f + static_cast<int64_t>(gy) * pitch + x) : 0.0f;
-    }
-  }
-}
-
 template <class TS, int OpK, int S>
 __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     fast2d_kernel(const __grid_constant__ CUtensorMap map_src, const __grid_constant__ CUtensorMap map_dst,
@@ -114,7 +32,6 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   constexpr int N = Vec<TS>::N;
   constexpr int LW = 32 * N;
   constexpr int LH = (kFastThreads / 32) * S + 2;
-  constexpr bool kAdvect = (OpK == 3);
   constexpr size_t kBuf = (static_cast<size_t>(LW) * LH * sizeof(TS) + 127) & ~size_t(127);
   constexpr uint32_t kTileBytes = static_cast<uint32_t>(LW * LH * sizeof(TS));
   // dynamic shared memory, 128-byte aligned for TMA; derived pointers stay
@@ -132,9 +49,6 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   (void)map_v;
 
   const int tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  const int x0 = lane * N;           // this thread's column vector
-  const int yb = 1 + warp * S;       // first row of this warp's strip
   if (tid == 0) {
     for (int i = 0; i < kFastBufs; ++i) mbar_init(&bars[i], 1);
     fence_barrier_init();
@@ -149,8 +63,6 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   for (int n = 0; n < 9; ++n) wt[n] = (n < shp.n) ? p.wt[n] : 0.0f;
 
   TS* dst = static_cast<TS*>(p.dst);
-  const TS* wu = static_cast<const TS*>(p.u);
-  const TS* wv = static_cast<const TS*>(p.v);
   uint32_t phase_bits = 0;  // bit i: parity of the next completion of bars[i]
   const int ntiles = p.tiles_x * p.tiles_y;
   auto origin = [&](int t, int& gy0, int& gx0) {
@@ -195,98 +107,22 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     if (stage_dst) phase_bits ^= (1u << bp);
     if (!__syncthreads_and(ok)) return;
 
-    const int gxv = gx0 + x0;
-    for (int s = 1; s <= p.steps; ++s) {
-      const TS* in = buf((s & 1) ? bs : bp);
-      TS* out = buf((s & 1) ? bp : bs);
-      // window: rows yb-1 .. yb+S, each [left, v0..v3, right]; the left and
-      // right neighbours come from the adjacent lanes (one warp spans a row)
-      float win[S + 2][N + 2];
-#pragma unroll
-      for (int k = 0; k < S + 2; ++k) {
-        ld_vec(in + (yb - 1 + k) * LW + x0, &win[k][1]);
-        win[k][0] = __shfl_up_sync(0xFFFFFFFFu, win[k][N], 1);
-        win[k][N + 1] = __shfl_down_sync(0xFFFFFFFFu, win[k][1], 1);
-      }
-#pragma unroll
-      for (int k = 1; k <= S; ++k) {
-        const int y = yb - 1 + k;
-        float res[N];
-        if constexpr (!kAdvect) {
-#pragma unroll
-          for (int c = 0; c < N; ++c) {
-            float acc = __fmul_rn(wt[0], win[k + shp.dh[0]][1 + c + shp.dw[0]]);
-#pragma unroll
-            for (int n = 1; n < shp.n; ++n) acc = __fadd_rn(acc, __fmul_rn(wt[n], win[k + shp.dh[n]][1 + c + shp.dw[n]]));
-            res[c] = acc;
-          }
-        } else {
-          float uu[N], vv[N];
-          ld_wind(wu, p.pitch, gy0 + y, gxv, p.W, p.H, uu);
-          ld_wind(wv, p.pitch, gy0 + y, gxv, p.W, p.H, vv);
-#pragma unroll
-          for (int c = 0; c < N; ++c) {
-            const float cc = win[k][1 + c];
-            const float n_ = win[k - 1][1 + c];
-            const float e_ = win[k][2 + c];
-            const float w_ = win[k][c];
-            const float s_ = win[k + 1][1 + c];
-            const float sum = __fsub_rn(__fmul_rn(4.0f, cc), __fadd_rn(__fadd_rn(__fadd_rn(n_, e_), w_), s_));
-            const float xw = uu[c], yw = vv[c];
-            const float cvy = (yw > 0.0f) ? yw : -yw;  // yf * yw with yf = +-1
-            const float cvx = (xw > 0.0f) ? xw : -xw;
-            const float nbx = (xw > 0.0f) ? e_ : w_;
-            const float nby = (yw > 0.0f) ? s_ : n_;
-            const float temp_wind = __fsub_rn(__fmul_rn(-cvx, __fmul_rn(__fsub_rn(cc, nbx), p.inv_dx)),
-                                              __fmul_rn(cvy, __fmul_rn(__fsub_rn(cc, nby), p.inv_dx)));
-            const float cond = __fmul_rn(__fmul_rn(-p.K, __fmul_rn(sum, 0.25f)), p.dt);
-            res[c] = __fadd_rn(__fadd_rn(cc, cond), __fmul_rn(temp_wind, p.dt));
-          }
-        }
-        TS* o = out + y * LW + x0;
-        if (ring_tile) {
-          // cells outside r <= h < H-r, r <= w < W-r keep this buffer's value
-          const int gy = gy0 + y;
-          const bool row_in = gy >= p.ring && gy < p.H - p.ring;
-          float old[N];
-          ld_vec(o, old);
-#pragma unroll
-          for (int c = 0; c < N; ++c) {
-            const int gx = gxv + c;
-            if (!(row_in && gx >= p.ring && gx < p.W - p.ring)) res[c] = old[c];
-          }
-        }
-        st_vec(o, res);
-      }
-      __syncthreads();
-    }
-
-    // core -> global, interior cells only, vector stores
-    const TS* fin = buf((p.steps & 1) ? bp : bs);
-    const int vpr = p.TW / N;
-    for (int i = tid; i < p.TH * vpr; i += kFastThreads) {
-      const int r = i / vpr;
-      const int cv = i - r * vpr;
-      const int y = p.HY + r, x = p.HX + cv * N;
-      const int gy = gy0 + y, gx = gx0 + x;
-      if (gy < p.ring || gy >= p.H - p.ring) continue;
-      if (gx + N <= p.ring || gx >= p.W - p.ring) continue;
-      TS* d = dst + static_cast<int64_t>(gy) * p.pitch + gx;
-      const TS* sp = fin + y * LW + x;
-      constexpr int kVecBytes = N * static_cast<int>(sizeof(TS));
-      if (gx >= p.ring && gx + N <= p.W - p.ring && (reinterpret_cast<uintptr_t>(d) & (kVecBytes - 1)) == 0) {
-        if constexpr (kVecBytes == 16)
-          *reinterpret_cast<uint4*>(d) = *reinterpret_cast<const uint4*>(sp);
-        else
-          *reinterpret_cast<uint2*>(d) = *reinterpret_cast<const uint2*>(sp);
-      } else {
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-          const int xx = gx + k;
-          if (xx >= p.ring && xx < p.W - p.ring) d[k] = sp[k];
-        }
-      }
-    }
+    TileGeom g;
+    g.W = p.W;
+    g.H = p.H;
+    g.ring = p.ring;
+    g.steps = p.steps;
+    g.TW = p.TW;
+    g.TH = p.TH;
+    g.HX = p.HX;
+    g.HY = p.HY;
+    g.pitch = p.pitch;
+    g.K = p.K;
+    g.dt = p.dt;
+    g.inv_dx = p.inv_dx;
+    g.u = p.u;
+    g.v = p.v;
+    fast2d_run_tile<TS, OpK, S>(buf(bs), buf(bp), dst, g, gy0, gx0, ring_tile, wt);
     __syncthreads();
   }
 }

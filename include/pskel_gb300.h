@@ -163,6 +163,36 @@ PSKEL_API pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_
                                         const pskel_schedule* sched, int64_t residual_every,
                                         double* residuals_host);
 
+/* ---------------------------------------------------------------- batches
+ * Many 2D grids, each with its own size, iteration count and schedule, run by
+ * ONE persistent kernel launch recorded once in a CUDA graph. There is no
+ * counterpart in the reference, whose skeletons run one grid per call
+ * (StencilBase::runIterativeGPU, PSkelStencil.hpp:1046-1097); a batch gives
+ * every grid exactly the result pskel_iterate2d would (in `out` for an odd
+ * iteration count, in `in` for an even one). The stencil must be a linear
+ * mask of reach 1 in one of the shapes N,S,W,E / C,N,S,W,E / 3x3 row-major,
+ * storage f32 or bf16, buffers and row pitches 16-byte aligned. */
+typedef struct pskel_batch_grid {
+  void* in;                /* device buffer, 16-byte aligned */
+  void* out;               /* device buffer, 16-byte aligned */
+  int64_t width, height;   /* grid size */
+  int64_t pitch;           /* row pitch in elements (0 = width) */
+  int64_t iterations;      /* steps for this grid */
+  pskel_schedule schedule; /* time_steps used (0 = default) */
+} pskel_batch_grid;
+
+typedef struct pskel_batch pskel_batch;
+
+/* Prepares a batch: per-grid geometry, tensor maps, the work list and the
+ * CUDA graph of the run. The grids' buffers must stay valid until destroy. */
+PSKEL_API pskel_status pskel_batch_create(const pskel_stencil* st, const pskel_batch_grid* grids, int32_t n,
+                                          pskel_batch** out);
+/* Launches the batch's graph on `stream` (asynchronous; see pskel_sync). */
+PSKEL_API pskel_status pskel_batch_run(pskel_batch* b, void* stream);
+/* Total cell updates of one run (sum of width * height * iterations). */
+PSKEL_API int64_t pskel_batch_cell_updates(const pskel_batch* b);
+PSKEL_API pskel_status pskel_batch_destroy(pskel_batch* b);
+
 /* pskel_iterate3d without any allocation by the library. It has no
  * counterpart in the reference: it serves callers that cannot let a library
  * call cudaMalloc, such as a host application that owns all device memory

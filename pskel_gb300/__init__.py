@@ -45,6 +45,11 @@ class Schedule(C.Structure):
                 ("ctas", C.c_int32)]
 
 
+class BatchGrid(C.Structure):
+    _fields_ = [("in_", C.c_void_p), ("out", C.c_void_p), ("width", C.c_int64), ("height", C.c_int64),
+                ("pitch", C.c_int64), ("iterations", C.c_int64), ("schedule", Schedule)]
+
+
 def _load():
     if not LIB_PATH.exists():
         raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
@@ -60,6 +65,11 @@ def _load():
                                      C.POINTER(Schedule)]
     lib.pskel_iterate3d.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                     C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p, C.c_void_p]
+    lib.pskel_batch_create.argtypes = [C.POINTER(Stencil), C.POINTER(BatchGrid), C.c_int32, C.POINTER(C.c_void_p)]
+    lib.pskel_batch_run.argtypes = [C.c_void_p, C.c_void_p]
+    lib.pskel_batch_cell_updates.argtypes = [C.c_void_p]
+    lib.pskel_batch_cell_updates.restype = C.c_int64
+    lib.pskel_batch_destroy.argtypes = [C.c_void_p]
     lib.pskel_iterate3d_noalloc.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                             C.c_int64, C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p,
                                             C.c_void_p]
@@ -170,3 +180,42 @@ def run3d_host(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int
     _check(lib.pskel_run3d_host(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, D, iterations,
                                 C.byref(sc) if sc is not None else None, residual_every, res.ctypes.data))
     return a_out, res[:n]
+
+
+class Batch:
+    """Many 2D grids in one persistent launch (a CUDA graph). `grids` is a list
+    of (in, out, iterations, time_steps) with torch CUDA tensors [H][W] or
+    (in, out, iterations, time_steps, pitch)."""
+
+    def __init__(self, st: Stencil, grids):
+        arr = (BatchGrid * len(grids))()
+        for i, g in enumerate(grids):
+            a, b, iters, T = g[:4]
+            pitch = g[4] if len(g) > 4 else 0
+            arr[i].in_ = _ptr(a)
+            arr[i].out = _ptr(b)
+            arr[i].height, arr[i].width = a.shape[0], (g[5] if len(g) > 5 else a.shape[1])
+            arr[i].pitch = pitch
+            arr[i].iterations = iters
+            arr[i].schedule = Schedule(time_steps=T)
+        self._st = st
+        self.handle = C.c_void_p()
+        _check(lib.pskel_batch_create(C.byref(st), arr, len(grids), C.byref(self.handle)))
+
+    def run(self, stream=None):
+        _check(lib.pskel_batch_run(self.handle, stream))
+
+    @property
+    def cell_updates(self) -> int:
+        return lib.pskel_batch_cell_updates(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib.pskel_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -193,6 +193,65 @@ PSKEL_API pskel_status pskel_batch_run(pskel_batch* b, void* stream);
 PSKEL_API int64_t pskel_batch_cell_updates(const pskel_batch* b);
 PSKEL_API pskel_status pskel_batch_destroy(pskel_batch* b);
 
+/* --------------------------------------------------------- schedule search
+ * Replaces runIterativeAutoGPU's genetic search (PSkelStencil.hpp:1865-2076),
+ * which needs GAlib and evaluates an analytic objective, with measured
+ * timings and a learned cost model. None of these change results. */
+
+/* Candidate schedules the library can run for this 2D stencil; writes at most
+ * `cap` to `out` and returns how many there are. Host only. */
+PSKEL_API int32_t pskel_candidates2d(const pskel_stencil* st, int64_t width, int64_t height, int64_t iterations,
+                                     pskel_schedule* out, int32_t cap);
+
+/* Times `n` schedules on device buffers (their contents are overwritten): one
+ * untimed run each, then the median of `reps` runs in ms, CUDA events on
+ * `stream`. The exhaustive tuner is this over pskel_candidates2d. */
+PSKEL_API pskel_status pskel_time2d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height,
+                                    int64_t pitch, int64_t iterations, const pskel_schedule* scheds, int32_t n,
+                                    int32_t reps, double* ms, void* stream);
+
+/* The reference's GA with its analytic objective (solve2D/objective2D,
+ * PSkelStencil.hpp:1883-1941: simple GA, two 16-bit genes, population
+ * `popsize`, `ngen` generations, pmut 0.01, pcross 0.6), its (tile height,
+ * steps) pick mapped onto this library's schedule. Host only. */
+PSKEL_API pskel_status pskel_ga_schedule2d(const pskel_stencil* st, int64_t width, int64_t height, int64_t iterations,
+                                           uint64_t seed, int32_t popsize, int32_t ngen, pskel_schedule* out,
+                                           double* score);
+
+/* The 8 cost-model input features of one (grid, schedule); returns 8. */
+PSKEL_API int32_t pskel_schedule_features2d(const pskel_stencil* st, int64_t width, int64_t height,
+                                            int64_t iterations, const pskel_schedule* s, float* out);
+
+/* The schedule runIterativeAutoGPU uses: the candidate with the lowest time
+ * predicted by the registered cost model (pskel_set_cost_model, or the file
+ * named by the PSKEL_COST_MODEL environment variable), else the default. */
+PSKEL_API pskel_status pskel_auto_schedule2d(const pskel_stencil* st, int64_t width, int64_t height,
+                                             int64_t iterations, pskel_schedule* out);
+
+/* ------------------------------------------------------------- cost model
+ * A small MLP (dense tanh layers, linear output) trained and evaluated by this
+ * library's CUDA kernels (forward, backward, Adam; full-batch MSE). */
+typedef struct pskel_mlp pskel_mlp;
+PSKEL_API pskel_status pskel_mlp_create(int32_t in_dim, int32_t hidden, int32_t layers, uint64_t seed,
+                                        pskel_mlp** out);
+PSKEL_API int64_t pskel_mlp_num_params(const pskel_mlp* m);
+PSKEL_API void pskel_mlp_shape(const pskel_mlp* m, int32_t* in_dim, int32_t* hidden, int32_t* layers);
+PSKEL_API pskel_status pskel_mlp_get_params(const pskel_mlp* m, float* host);
+PSKEL_API pskel_status pskel_mlp_set_params(pskel_mlp* m, const float* host);
+/* y[n] = model(x[n][in_dim]) (host arrays) */
+PSKEL_API pskel_status pskel_mlp_predict(pskel_mlp* m, const float* x_host, int32_t n, float* y_host);
+/* gradient of mean((model(x) - y)^2) w.r.t. the parameters, and that loss */
+PSKEL_API pskel_status pskel_mlp_gradient(pskel_mlp* m, const float* x_host, const float* y_host, int32_t n,
+                                          float* grads_host, float* loss);
+/* `epochs` full-batch Adam steps with learning rate lr; final loss */
+PSKEL_API pskel_status pskel_mlp_train(pskel_mlp* m, const float* x_host, const float* y_host, int32_t n,
+                                       int32_t epochs, float lr, float* final_loss);
+PSKEL_API pskel_status pskel_mlp_save(const pskel_mlp* m, const char* path);
+PSKEL_API pskel_status pskel_mlp_load(const char* path, pskel_mlp** out);
+PSKEL_API pskel_status pskel_mlp_destroy(pskel_mlp* m);
+/* Registers the model pskel_auto_schedule2d uses (NULL: the default schedule). */
+PSKEL_API pskel_status pskel_set_cost_model(pskel_mlp* m);
+
 /* pskel_iterate3d without any allocation by the library. It has no
  * counterpart in the reference: it serves callers that cannot let a library
  * call cudaMalloc, such as a host application that owns all device memory

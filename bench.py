@@ -6,7 +6,7 @@ per step, temporal blocking of 16 generations per pass. A "step" is one full
 1000-generation run over the grid.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload life|jacobi|advect|advect_bf16|jacobi_bf16]
+                    [--workload life|jacobi|jacobi_bf16|advect|advect_bf16|heat3d|heat3d_bf16|batch|batch_bf16]
 
 Prints ONE JSON line. ``value`` is GCells/s (cell updates per second) with the
 grid resident in HBM; ``e2e`` is the same metric through the host entry point
@@ -49,10 +49,17 @@ WORKLOADS = {
     "advect_bf16": dict(desc="advection-diffusion 2D, bf16 storage / fp32 arithmetic, 4096x4096, 500 iterations",
                         W=4096, H=4096, iters=500, dtype="bf16", T=4, b_alg=8),
     "heat3d": dict(desc="3D 7-point heat (Mask3D), float32 512^3, zero halo, 50 iterations, fp64 residual every 10",
-                   W=512, H=512, D=512, iters=50, dtype="f32", T=2, b_alg=8, every=10),
+                   W=512, H=512, D=512, iters=50, dtype="f32", T=1, b_alg=8, every=10),
     "heat3d_bf16": dict(desc="3D 7-point heat, bf16 storage / fp32 arithmetic, 512^3, 50 iterations, "
-                             "fp64 residual every 10", W=512, H=512, D=512, iters=50, dtype="bf16", T=2, b_alg=4,
+                             "fp64 residual every 10", W=512, H=512, D=512, iters=50, dtype="bf16", T=1, b_alg=4,
                         every=10),
+    "batch": dict(desc="batched Jacobi 2D 5-point, float32, 256 grids, sides log-uniform [64,2048], iterations "
+                       "uniform [10,500], one persistent launch in a CUDA graph, MLP-picked steps per pass",
+                  grids=256, train_grids=64, dtype="f32", batch=True, W=1024, H=1024, iters=100),
+    "batch_bf16": dict(desc="batched Jacobi 2D 5-point, bf16 storage / fp32 arithmetic, 256 grids, sides "
+                            "log-uniform [64,2048], iterations uniform [10,500], one persistent launch in a CUDA "
+                            "graph, MLP-picked steps per pass",
+                       grids=256, train_grids=64, dtype="bf16", batch=True, W=1024, H=1024, iters=100),
 }
 
 
@@ -152,7 +159,7 @@ def make_inputs(wl):
     if name == "life":
         a, b = S.life(W, H, seed=1)
         return {"in": a, "out": b}
-    if name.startswith("jacobi"):
+    if name.startswith("jacobi") or name.startswith("batch"):
         a, b = S.jacobi2d(W, H, seed=1)
         if wl["dtype"] == "bf16":
             a, b = S.f32_to_bf16(a), S.f32_to_bf16(b)
@@ -339,6 +346,219 @@ def run_ours(args, wl, world, rank, local):
     return line, clk.summary()
 
 
+# ------------------------------------------------- batched workload
+
+def batch_pool(torch, dev, shapes, dtype, seed):
+    """All grids of a batch in one device pool (each buffer 256-byte aligned,
+    rows padded to 16 bytes); returns the pool, its pristine copy and per-grid
+    (in view, out view, pitch)."""
+    from pskel_gb300 import synth as S
+    esz = 2 if dtype == "bf16" else 4
+    offs, total = [], 0
+    for W, H, _ in shapes:
+        pitch = -(-W * esz // 16) * 16 // esz
+        n = pitch * H
+        a_off = total
+        total += -(-n * esz // 256) * 256 // esz
+        b_off = total
+        total += -(-n * esz // 256) * 256 // esz
+        offs.append((a_off, b_off, pitch))
+    host = np.zeros(total, dtype=np.int16 if dtype == "bf16" else np.float32)
+    for k, ((W, H, _), (a_off, b_off, pitch)) in enumerate(zip(shapes, offs)):
+        a, b = S.jacobi2d(W, H, seed=seed * 100003 + k)
+        if dtype == "bf16":
+            a, b = S.f32_to_bf16(a).view(np.int16), S.f32_to_bf16(b).view(np.int16)
+        host[a_off:a_off + pitch * H].reshape(H, pitch)[:, :W] = a
+        host[b_off:b_off + pitch * H].reshape(H, pitch)[:, :W] = b
+    pool0 = torch.from_numpy(host).to(dev)
+    pool = pool0.clone()
+    views = [(pool[a:a + p * H].view(H, p), pool[b:b + p * H].view(H, p), p)
+             for (W, H, _), (a, b, p) in zip(shapes, offs)]
+    return host, pool, pool0, views
+
+
+def run_batch(args, wl, world, rank, local):
+    """256 Jacobi grids of uneven shapes and iteration counts in one
+    persistent launch (a CUDA graph). The per-grid steps per pass come from the
+    MLP cost model (trained here on timings the measured tuner takes on a
+    separate set of grids); the same batch with the exhaustive tuner's picks,
+    and the GA-tuned plain per-grid launches, are timed beside it."""
+    import torch
+
+    import pskel_gb300 as P
+    import pskel_gb300.tuner as T
+    from pskel_gb300 import synth as S
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dtype = wl["dtype"]
+    esz = 2 if dtype == "bf16" else 4
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    shapes = S.batch_shapes(wl["grids"], seed=1 + rank)
+    cells = sum(W * H * it for W, H, it in shapes)
+    host, pool, pool0, views = batch_pool(torch, dev, shapes, dtype, seed=1 + rank)
+
+    def cands(W, H, it):  # the batched kernel's space: steps per pass on the 128 x 66 tile
+        return [c for c in T.candidates(st, W, H, it) if c.tile_h == 0]
+
+    # ---- tuning (untimed). Measured tuner on the benchmark's grids.
+    t0 = time.perf_counter()
+    exh, exh_ms = [], []
+    for (W, H, it), (x, y, p) in zip(shapes, views):
+        cs = cands(W, H, it)
+        ms = T.time_schedules(st, x, y, it, cs, reps=3, pitch=p, width=W, height=H, stream=sp)
+        exh.append(cs[int(np.argmin(ms))].time_steps)
+        exh_ms.append(float(ms.min()))
+    t_exh = time.perf_counter() - t0
+    # training set: the same tuner's timings on a separate draw of grids
+    t0 = time.perf_counter()
+    tshapes = S.batch_shapes(wl["train_grids"], seed=1000 + rank)
+    _, _, _, tviews = batch_pool(torch, dev, tshapes, dtype, seed=1000 + rank)
+    X, Y = [], []
+    for (W, H, it), (x, y, p) in zip(tshapes, tviews):
+        cs = cands(W, H, it)
+        ms = T.time_schedules(st, x, y, it, cs, reps=3, pitch=p, width=W, height=H, stream=sp)
+        for c, m in zip(cs, ms):
+            X.append(T.features(st, W, H, it, c))
+            Y.append(np.log(m))
+    del tviews
+    X = np.stack(X)
+    Y = np.array(Y, dtype=np.float32)
+    model = T.CostModel(hidden=64, layers=3, seed=1)
+    y_mean = float(Y.mean())
+    loss = model.train(X, Y - y_mean, epochs=4000, lr=3e-3)
+    t_train = time.perf_counter() - t0
+    if args.save_model and rank == 0:
+        model.save(args.save_model)
+    learned = []
+    for W, H, it in shapes:
+        cs = cands(W, H, it)
+        pred = model.predict(np.stack([T.features(st, W, H, it, c) for c in cs]))
+        learned.append(cs[int(np.argmin(pred))].time_steps)
+    model.close()
+    ga = [T.ga_schedule(st, W, H, it, seed=1)[0] for W, H, it in shapes]
+
+    def make(ts):
+        return P.Batch(st, [(x, y, it, t, p, W) for (W, H, it), (x, y, p), t in zip(shapes, views, ts)])
+
+    b_learned = make(learned)
+    b_exh = make(exh)
+    b_default = make([0] * len(shapes))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+
+    def reset():
+        with torch.cuda.stream(stream):
+            pool.copy_(pool0)
+            flush.fill_(1)
+
+    def ga_plain():
+        for (W, H, it), (x, y, p), s in zip(shapes, views, ga):
+            P.iterate2d(st, x, y, it, sched=s, pitch=p, width=W, height=H, stream=sp)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            reset()
+            fn()
+        P.sync(sp)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize()
+        dist_barrier(world)
+        for s, e in ev:
+            reset()
+            s.record(stream)
+            fn()
+            e.record(stream)
+        P.sync(sp)
+        torch.cuda.synchronize()
+        dist_barrier(world)
+        return dist_max(sum(s.elapsed_time(e) for s, e in ev) / 1e3, world)
+
+    with ClockSampler(local) as clk:
+        t_learned = timed(lambda: b_learned.run(sp), args.steps, args.warmup)
+    t_exh_b = timed(lambda: b_exh.run(sp), args.steps, args.warmup)
+    t_def = timed(lambda: b_default.run(sp), args.steps, args.warmup)
+    t_ga = timed(ga_plain, max(1, args.steps // 2), 1)
+    ga_steps = max(1, args.steps // 2)
+
+    # result check: the learned and exhaustive batches give identical grids
+    reset()
+    b_learned.run(sp)
+    P.sync(sp)
+    res_l = pool.clone()
+    reset()
+    b_exh.run(sp)
+    P.sync(sp)
+    same = bool(torch.equal(res_l, pool))
+
+    # ---- end to end: pinned host grids in, one graph launch, results out
+    pin_src = torch.from_numpy(host).pin_memory()
+    pin_res = torch.empty_like(pin_src).pin_memory()
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            pool.copy_(pin_src, non_blocking=True)
+        b_learned.run(sp)
+        with torch.cuda.stream(stream):
+            pin_res.copy_(pool, non_blocking=True)
+        stream.synchronize()
+
+    for _ in range(args.warmup):
+        e2e_step()
+    tt = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        e2e_step()
+        tt.append(time.perf_counter() - t1)
+    t_e2e = dist_max(sum(tt), world)
+    pool_bytes = pool.numel() * esz
+
+    value = world * cells * args.steps / t_learned / 1e9
+    v_exh = world * cells * args.steps / t_exh_b / 1e9
+    v_def = world * cells * args.steps / t_def / 1e9
+    v_ga = world * cells * ga_steps / t_ga / 1e9
+    peak, peak_kind = load_peaks()
+    # one launch per step: algorithmic bytes = B_alg x every cell update of the batch
+    b_alg = 2 * esz
+    per_launch = t_learned / args.steps
+    achieved = b_alg * cells / per_launch / 1e9
+    passes = sum(P.lib.pskel_plan_passes(it, t, None, 0) for (W, H, it), t in zip(shapes, learned))
+    pass_bytes = sum(2 * esz * W * H * P.lib.pskel_plan_passes(it, t, None, 0)
+                     for (W, H, it), t in zip(shapes, learned))
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_learned / args.steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded SplitMix64)",
+        "config": {"workload": wl["desc"], "grids": len(shapes), "cell_updates_per_step": cells,
+                   "l2": "flushed between timed steps (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "tuning": {"learned_batch": round(value, 3), "exhaustive_batch": round(v_exh, 3),
+                   "default_batch": round(v_def, 3), "ga_plain_launches": round(v_ga, 3),
+                   "learned_vs_exhaustive": round(value / v_exh, 4), "learned_vs_ga_plain": round(value / v_ga, 4),
+                   "picks_equal_exhaustive": int(sum(a == b for a, b in zip(learned, exh))),
+                   "exhaustive_tuning_s": round(t_exh, 2), "training_s": round(t_train, 2),
+                   "training_samples": int(X.shape[0]), "training_loss": round(float(loss), 5),
+                   "results_identical": same},
+        "e2e": {"value": round(world * cells * args.steps / t_e2e / 1e9, 3), "unit": "GCells/s",
+                "h2d_bytes_per_step": pool_bytes, "d2h_bytes_per_step": pool_bytes},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 3), "traffic": load_traffic(wl["name"]),
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s",
+                     "per_launch_ms": round(per_launch * 1e3, 4), "passes_per_launch": passes,
+                     "pass_compulsory_frac": round(pass_bytes / per_launch / 1e9 / peak, 3),
+                     "note": "one persistent launch runs every pass of every grid; achieved = B_alg x cell "
+                             "updates / launch time; pass_compulsory_frac = one read + one write of each grid per "
+                             "pass / launch time / peak"},
+    }
+    for b in (b_learned, b_exh, b_default):
+        b.close()
+    return line, clk.summary()
+
+
 def plan_any(iters, T):
     """Pass lengths of a 3D run (mirror of the library's plan for fully written grids)."""
     p = [T] * (iters // T) + ([iters % T] if iters % T else [])
@@ -383,7 +603,7 @@ def cpu_sample(wl, threads, iters_sample, use_ref=True):
                                                                                               S.HEAT7_WEIGHTS)))
                 cmd = ["lin3d", wl["dtype"], W, H, wl["D"], iters_sample, threads, d / "m.txt", "0.0", d / "in",
                        d / "out", d / "res"]
-            elif wl["name"].startswith("jacobi"):
+            elif wl["name"].startswith(("jacobi", "batch")):
                 with open(d / "m.txt", "w") as f:
                     f.write("4 2\n" + "".join(f"{o[0]} {o[1]} {w!r}\n" for o, w in zip(S.JACOBI4_OFFSETS,
                                                                                      S.JACOBI4_WEIGHTS)))
@@ -400,7 +620,7 @@ def cpu_sample(wl, threads, iters_sample, use_ref=True):
     t0 = time.perf_counter()
     if wl["name"] == "life":
         oracle.life(x["in"], x["out"], iters_sample)
-    elif wl["name"].startswith("jacobi"):
+    elif wl["name"].startswith(("jacobi", "batch")):
         from pskel_gb300 import synth as S
         oracle.lin2d(x["in"], x["out"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters_sample, dtype=wl["dtype"])
     elif wl["name"].startswith("heat3d"):
@@ -436,6 +656,9 @@ def run_reference_arm(args, wl, world, rank):
     value = cells / sum(walls) / 1e9
     shape = "x".join(str(v) for v in ([wl["H"], wl["W"]] + ([wl["D"]] if "D" in wl else [])))
     sample = f"{shape} grid, {its} iterations per step (of {wl['iters']}), {threads} OpenMP threads"
+    if wl.get("batch"):
+        sample = (f"one {shape} grid of the same stencil, {its} iterations per step (the reference has no batched "
+                  f"path: runIterativeCPU runs grid by grid), {threads} OpenMP threads")
     return {"metric": METRIC, "value": round(value, 4), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(sum(walls) / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",
@@ -456,6 +679,7 @@ def main():
     ap.add_argument("--time-steps", type=int, default=0)
     ap.add_argument("--tile-h", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--save-model", default="", help="batch workloads: write the trained cost model here")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload], name=args.workload)
     world, rank, local = dist_setup()
@@ -464,7 +688,8 @@ def main():
         if line is not None:
             print(json.dumps(line), flush=True)
         return
-    line, clocks = run_ours(args, wl, world, rank, local)
+    runner = run_batch if wl.get("batch") else run_ours
+    line, clocks = runner(args, wl, world, rank, local)
     line["clocks"] = clocks
     if rank == 0:
         if not args.no_cpu_baseline:

@@ -345,6 +345,28 @@ class Stencil2D : public StencilBase<Array, Mask, Args> {
     this->args = _args;
   }
 
+  // runIterativeAutoGPU's schedule for the library's stencils: the pick of the
+  // registered cost model (pskel_set_cost_model or the PSKEL_COST_MODEL file)
+  // among the library's candidates, else the library default.
+  pskel_schedule autoSchedule(size_t iterations) override {
+    constexpr int op = StencilOp<Args>::value;
+    constexpr int dt = detail::LibDtype<T>::value;
+    pskel_schedule s = detail::make_schedule(0, 0, 0, 0);
+    if constexpr (op != kUserFunctor && dt >= 0) {
+      std::vector<int32_t> off;
+      std::vector<float> wt;
+      pskel_stencil st;
+      std::memset(&st, 0, sizeof(st));
+      st.op = static_cast<pskel_op>(op);
+      st.dtype = static_cast<pskel_dtype>(dt);
+      st.mask = detail::describe_mask(this->mask, off, wt);
+      pskelErrchk(pskel_auto_schedule2d(&st, static_cast<int64_t>(this->input.getWidth()),
+                                        static_cast<int64_t>(this->input.getHeight()),
+                                        static_cast<int64_t>(iterations), &s));
+    }
+    return s;
+  }
+
  protected:
   void runGPUSchedule(size_t iterations, pskel_schedule sched) override {
     constexpr int op = StencilOp<Args>::value;

@@ -218,7 +218,11 @@ PSKEL_API pskel_status pskel_ga_schedule2d(const pskel_stencil* st, int64_t widt
                                            uint64_t seed, int32_t popsize, int32_t ngen, pskel_schedule* out,
                                            double* score);
 
-/* The 8 cost-model input features of one (grid, schedule); returns 8. */
+/* The 11 cost-model input features of one (grid, schedule): log2 width,
+ * log2 height, log2 iterations, steps per pass / 8, tall-tile flag, bytes per
+ * cell / 4, op, log2 passes, log2 of the redundant-halo factor (loaded tile
+ * area / core tile area), log2 tiles per pass, log2 cell updates including
+ * the redundant ones. Writes 11 floats and returns 11. Host only. */
 PSKEL_API int32_t pskel_schedule_features2d(const pskel_stencil* st, int64_t width, int64_t height,
                                             int64_t iterations, const pskel_schedule* s, float* out);
 

@@ -49,6 +49,69 @@ struct Rng {
   double uniform() { return static_cast<double>(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
+constexpr int kFeatures = 11;
+
+// Tile geometry a schedule gets (the selection rules of the Life, register-
+// windowed and generic 2D paths in capi.cu), for the cost-model features.
+struct TileEstimate {
+  int T;           // steps per pass after clamping
+  int TW, TH;      // core tile
+  int LW, LH;      // loaded tile (core + redundant halo)
+  bool tall;       // the taller tile variant
+  int64_t passes;
+};
+
+TileEstimate estimate_tiles(const pskel_stencil& st, int64_t W, int64_t H, int64_t iters, const pskel_schedule& s) {
+  TileEstimate g{};
+  const int64_t it = std::max<int64_t>(iters, 1);
+  auto clamp_odd = [&](int T, int tmax) {
+    T = static_cast<int>(std::min<int64_t>(std::min(T, tmax), it));
+    if (T > 1 && (T & 1) == 0) --T;
+    return std::max(T, 1);
+  };
+  if (st.op == PSKEL_OP_LIFE) {
+    g.T = clamp_odd(s.time_steps > 0 ? s.time_steps : 15, kLifeMaxT);
+    g.TH = std::max(2, (s.tile_h > 0 ? std::min(s.tile_h, 256 - 2 * g.T) : 256 - 2 * g.T) & ~1);
+    g.LH = g.TH + 2 * g.T;
+    g.TW = kLifeTW;
+    g.LW = kLifeLW;
+    g.tall = false;
+  } else if (fast_path(st)) {
+    const int vec = st.dtype == PSKEL_BF16 ? 8 : 4;
+    const int S = s.tile_h > 64 ? 8 : 4;
+    g.LW = 128;
+    g.LH = 16 * S + 2;
+    int T = clamp_odd(s.time_steps > 0 ? s.time_steps : (st.dtype == PSKEL_BF16 ? 7 : 3), 1 << 20);
+    int HX = 0;
+    for (;;) {
+      HX = ((T + vec - 1) / vec) * vec;
+      if ((g.LW - 2 * HX >= 4 && g.LH - 2 * T >= 2) || T == 1) break;
+      T -= 2;
+    }
+    g.T = T;
+    g.TW = g.LW - 2 * HX;
+    g.TH = g.LH - 2 * T;
+    g.tall = S == 8;
+  } else {
+    int R = 1;
+    if (st.mask.size > 0 && st.mask.offsets) {
+      R = 0;
+      for (int i = 0; i < 2 * st.mask.size; ++i) R = std::max(R, std::abs(st.mask.offsets[i]));
+    }
+    g.T = clamp_odd(s.time_steps > 0 ? s.time_steps : (st.op == PSKEL_OP_ADVECT ? 4 : 8), 1 << 20);
+    if (R == 0) g.T = 1;
+    g.TW = s.tile_w > 0 ? s.tile_w : 128;
+    g.TH = s.tile_h > 0 ? s.tile_h : 64;
+    g.LW = g.TW + 2 * R * g.T;
+    g.LH = g.TH + 2 * R * g.T;
+    g.tall = g.TH > 64;
+  }
+  g.TW = std::max(g.TW, 1);
+  g.TH = std::max(g.TH, 1);
+  g.passes = static_cast<int64_t>(plan_passes(it, g.T).size());
+  return g;
+}
+
 pskel_mlp* g_model = nullptr;
 bool g_model_env_tried = false;
 
@@ -150,7 +213,7 @@ pskel_status pskel_ga_schedule2d(const pskel_stencil* st, int64_t width, int64_t
   const double div = (2.0 * tile_w * H * type_size) / (mem_free * 1.1);
   const double max_h = std::max(1.0, std::ceil(H / std::max(div, 1e-12)));
   auto objective = [&](double h, double it) {
-    const double tile_h = std::min(H, 2.0 * it * R + h);
+    const double tile_h = std::floor(std::min(H, 2.0 * it * R + h));  // a size_t in the reference
     if (2.0 * tile_w * tile_h * type_size > mem_free) return 0.0;
     return (h / tile_h) * ((it * h) / (H * I));
   };
@@ -238,24 +301,28 @@ pskel_status pskel_ga_schedule2d(const pskel_stencil* st, int64_t width, int64_t
 
 int32_t pskel_schedule_features2d(const pskel_stencil* st, int64_t width, int64_t height, int64_t iterations,
                                   const pskel_schedule* s, float* out) {
-  // [log2 W, log2 H, log2 iterations, steps per pass, tile-height class,
-  //  bytes per cell, op, log2 passes]; the MLP input for one candidate
+  // The MLP input for one candidate (kFeatures values):
+  //  [log2 W, log2 H, log2 iterations, steps per pass / 8, tall-tile flag,
+  //   bytes per cell / 4, op, log2 passes, log2 redundant-halo factor,
+  //   log2 tiles per pass, log2 cell updates including redundant ones]
   if (!st || !s || !out) return 0;
-  const int64_t it = std::max<int64_t>(iterations, 1);
-  int T = s->time_steps > 0 ? s->time_steps : 0;
-  if (T > it) T = static_cast<int>(it);
-  if (T > 1 && (T & 1) == 0) --T;
+  const TileEstimate g = estimate_tiles(*st, width, height, iterations, *s);
+  const double it = static_cast<double>(std::max<int64_t>(iterations, 1));
   const double esz = st->dtype == PSKEL_U8 ? 1.0 : (st->dtype == PSKEL_BF16 ? 2.0 : 4.0);
-  const double passes = T > 0 ? std::ceil(static_cast<double>(it) / T) : 0.0;
+  const double redundancy = (static_cast<double>(g.LW) * g.LH) / (static_cast<double>(g.TW) * g.TH);
+  const double tiles = std::ceil(static_cast<double>(width) / g.TW) * std::ceil(static_cast<double>(height) / g.TH);
   out[0] = static_cast<float>(std::log2(static_cast<double>(width)));
   out[1] = static_cast<float>(std::log2(static_cast<double>(height)));
-  out[2] = static_cast<float>(std::log2(static_cast<double>(it)));
-  out[3] = static_cast<float>(T) / 8.0f;
-  out[4] = s->tile_h > 64 ? 1.0f : 0.0f;
+  out[2] = static_cast<float>(std::log2(it));
+  out[3] = static_cast<float>(g.T) / 8.0f;
+  out[4] = g.tall ? 1.0f : 0.0f;
   out[5] = static_cast<float>(esz) / 4.0f;
   out[6] = static_cast<float>(st->op);
-  out[7] = static_cast<float>(std::log2(std::max(1.0, passes)));
-  return 8;
+  out[7] = static_cast<float>(std::log2(std::max(1.0, static_cast<double>(g.passes))));
+  out[8] = static_cast<float>(std::log2(redundancy));
+  out[9] = static_cast<float>(std::log2(tiles));
+  out[10] = static_cast<float>(std::log2(static_cast<double>(width) * height * it * redundancy));
+  return kFeatures;
 }
 
 pskel_status pskel_set_cost_model(pskel_mlp* m) {
@@ -329,8 +396,9 @@ pskel_status pskel_auto_schedule2d(const pskel_stencil* st, int64_t width, int64
   pskel_schedule cand[64];
   const int32_t n = std::min<int32_t>(64, pskel_candidates2d(st, width, height, iterations, cand, 64));
   if (n <= 0) return PSKEL_OK;
-  std::vector<float> x(static_cast<size_t>(n) * 8), y(n);
-  for (int32_t i = 0; i < n; ++i) pskel_schedule_features2d(st, width, height, iterations, &cand[i], &x[8 * i]);
+  std::vector<float> x(static_cast<size_t>(n) * kFeatures), y(n);
+  for (int32_t i = 0; i < n; ++i)
+    pskel_schedule_features2d(st, width, height, iterations, &cand[i], &x[static_cast<size_t>(kFeatures) * i]);
   if (pskel_status q = pskel_mlp_predict(g_model, x.data(), n, y.data())) return q;
   int32_t best = 0;
   for (int32_t i = 1; i < n; ++i)

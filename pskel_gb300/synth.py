@@ -94,7 +94,7 @@ HEAT7_OFFSETS = [(0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0,
 HEAT7_WEIGHTS = [1.0 - 6 * HEAT7_ALPHA] + [HEAT7_ALPHA] * 6
 
 # Stream ids, one per field, so fields never share random bits.
-S_GRID, S_WIND_U, S_WIND_V, S_BLOBS = 1, 3, 5, 7
+S_GRID, S_WIND_U, S_WIND_V, S_BLOBS, S_BATCH = 1, 3, 5, 7, 9
 
 
 def jacobi2d(W: int, H: int, seed: int = 1):
@@ -105,6 +105,18 @@ def jacobi2d(W: int, H: int, seed: int = 1):
     a[:, 0] = 0
     a[:, -1] = 0
     return a, a.copy()
+
+
+def batch_shapes(n: int, seed: int = 1, smin: int = 64, smax: int = 2048, imin: int = 10, imax: int = 500):
+    """[(W, H, iterations)] of a batched workload: sides log-uniform in
+    [smin, smax], iterations uniform in [imin, imax]."""
+    u = (u64(seed, S_BATCH, 3 * n) >> np.uint64(11)).astype(np.float64) * 2.0**-53
+    u = u.reshape(n, 3)
+    lo, hi = np.log(smin), np.log(smax)
+    W = np.minimum(smax, np.floor(np.exp(lo + (hi - lo) * u[:, 0]))).astype(int)
+    H = np.minimum(smax, np.floor(np.exp(lo + (hi - lo) * u[:, 1]))).astype(int)
+    it = np.minimum(imax, imin + np.floor((imax - imin + 1) * u[:, 2])).astype(int)
+    return [(int(w), int(h), int(i)) for w, h, i in zip(W, H, it)]
 
 
 def life(W: int, H: int, seed: int = 1, p: float = 0.3):

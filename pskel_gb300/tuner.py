@@ -20,7 +20,7 @@ import numpy as np
 
 import pskel_gb300 as P
 
-NFEAT = 8
+NFEAT = 11
 
 
 def _setup():
@@ -178,19 +178,3 @@ class CostModel:
             P.lib.pskel_mlp_destroy(self.h)
             self.h = C.c_void_p()
 
-
-def mlp_forward_reference(params: np.ndarray, X: np.ndarray, dims) -> np.ndarray:
-    """fp64 restatement of the library's MLP forward pass (for gradient checks)."""
-    p = params.astype(np.float64)
-    a = X.astype(np.float64)
-    off = 0
-    L = len(dims) - 1
-    for l in range(L):
-        din, dout = dims[l], dims[l + 1]
-        Wl = p[off:off + din * dout].reshape(dout, din)
-        off += din * dout
-        bl = p[off:off + dout]
-        off += dout
-        z = a @ Wl.T + bl
-        a = np.tanh(z) if l < L - 1 else z
-    return a[:, 0]

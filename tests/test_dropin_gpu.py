@@ -41,7 +41,7 @@ def app():
     return APP
 
 
-def run_app(app, scenario, a, b, iters, want_res=False):
+def run_app(app, scenario, a, b, iters, want_res=False, env=None):
     shape = a.shape
     H, W = shape[0], shape[1]
     D = shape[2] if len(shape) == 3 else 1
@@ -53,7 +53,7 @@ def run_app(app, scenario, a, b, iters, want_res=False):
                 str(d / "res")]
         if want_res:
             args.append(str(d / "norms"))
-        r = subprocess.run(args, capture_output=True, text=True)
+        r = subprocess.run(args, capture_output=True, text=True, env=env)
         assert r.returncode == 0, r.stderr
         res = np.fromfile(d / "res", dtype=a.dtype).reshape(shape)
         norms = np.fromfile(d / "norms", dtype=np.float64) if want_res else None
@@ -97,3 +97,21 @@ def test_dropin_heat3d(app, oracle_mod, scenario, iters):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     if norms is not None:
         np.testing.assert_allclose(norms, wnorms, rtol=1e-12, atol=0)
+
+
+def test_dropin_auto_with_cost_model(app, oracle_mod, tmp_path):
+    """runIterativeAutoGPU with a cost-model file named by PSKEL_COST_MODEL:
+    the model picks the schedule, the results stay the reference's."""
+    import os
+
+    import pskel_gb300.tuner as T
+    m = T.CostModel(hidden=64, layers=3, seed=3)
+    path = tmp_path / "model.pmlp"
+    m.save(str(path))
+    m.close()
+    env = dict(os.environ, PSKEL_COST_MODEL=str(path))
+    for iters in (7, 40):
+        a, b = jac(517, 389, iters)
+        got, _ = run_app(app, "jacobi_auto", a, b, iters, env=env)
+        want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

@@ -125,5 +125,5 @@ def test_heat3d_c4_size_vs_oracle_and_fp64_error(cuda, oracle_mod):
                                 dtype="f64")
     e32 = float(np.max(np.abs(g32 - ref64)))
     eb = float(np.max(np.abs(S.bf16_to_f32(gb) - ref64)))
-    print(f"\nheat3d 128^3 x50: max abs error vs fp64: fp32 {e32:.3e}, bf16 storage {eb:.3e}")
+    print(f"\nFP64-ERROR heat3d 128^3 x50: max abs fp32 {e32:.3e}, bf16 storage {eb:.3e}")
     assert e32 < 1e-5 and eb < 0.05

@@ -483,15 +483,30 @@ def run_batch(args, wl, world, rank, local):
     t_ga = timed(ga_plain, max(1, args.steps // 2), 1)
     ga_steps = max(1, args.steps // 2)
 
-    # result check: the learned and exhaustive batches give identical grids
+    # uniform steps per pass for the whole batch, every odd value: the best
+    # uniform schedule is the other exhaustive reference point
+    uniform = {}
+    for t in range(1, 16, 2):
+        bu = make([t] * len(shapes))
+        uniform[t] = world * cells * 3 / timed(lambda: bu.run(sp), 3, 1) / 1e9
+        bu.close()
+    t_uni = max(uniform, key=uniform.get)
+
+    # result check: the learned and exhaustive batches leave identical results
+    # (each grid's result buffer; the other buffer holds a schedule-dependent
+    # intermediate state)
+    def results():
+        return [(y if it % 2 else x)[:, :W].clone() for (W, H, it), (x, y, p) in zip(shapes, views)]
+
     reset()
     b_learned.run(sp)
     P.sync(sp)
-    res_l = pool.clone()
+    res_l = results()
     reset()
     b_exh.run(sp)
     P.sync(sp)
-    same = bool(torch.equal(res_l, pool))
+    same = all(bool(torch.equal(a, b)) for a, b in zip(res_l, results()))
+    del res_l
 
     # ---- end to end: pinned host grids in, one graph launch, results out
     pin_src = torch.from_numpy(host).pin_memory()
@@ -536,7 +551,11 @@ def run_batch(args, wl, world, rank, local):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "tuning": {"learned_batch": round(value, 3), "exhaustive_batch": round(v_exh, 3),
                    "default_batch": round(v_def, 3), "ga_plain_launches": round(v_ga, 3),
-                   "learned_vs_exhaustive": round(value / v_exh, 4), "learned_vs_ga_plain": round(value / v_ga, 4),
+                   "uniform_batch": {str(t): round(v, 3) for t, v in uniform.items()},
+                   "best_uniform": {"time_steps": t_uni, "value": round(uniform[t_uni], 3)},
+                   "learned_vs_exhaustive": round(value / v_exh, 4),
+                   "learned_vs_best_uniform": round(value / uniform[t_uni], 4),
+                   "learned_vs_ga_plain": round(value / v_ga, 4),
                    "picks_equal_exhaustive": int(sum(a == b for a, b in zip(learned, exh))),
                    "exhaustive_tuning_s": round(t_exh, 2), "training_s": round(t_train, 2),
                    "training_samples": int(X.shape[0]), "training_loss": round(float(loss), 5),

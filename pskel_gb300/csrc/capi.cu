@@ -540,6 +540,57 @@ pskel_status validate3d(const pskel_stencil* st, const void* in, const void* out
   return PSKEL_OK;
 }
 
+// The 7-point cross, one step per launch, planes staged by TMA: persistent
+// blocks over work items of (32 vectors of d) x 16 w x HC planes, about four
+// items per resident block.
+static pskel_status stream3d_cross7(const pskel_stencil& st, Stencil3DParams& p, void* in, void* out, int64_t W,
+                                    int64_t H, int64_t D, int64_t iters, const pskel_schedule* sched, int64_t every,
+                                    double* partials_override, int64_t partials_cap, DeviceContext* c,
+                                    cudaStream_t s) {
+  const int dtype = static_cast<int>(st.dtype);
+  const int esz = static_cast<int>(dtype_size(st.dtype));
+  const int per_sm = stream3d_tma_blocks_per_sm(dtype);
+  const int64_t resident = static_cast<int64_t>(per_sm) * c->sms;
+  const int64_t cols = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), 1, esz);
+  int64_t chunks = std::max<int64_t>(1, (4 * resident + cols - 1) / cols);
+  chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / 8));
+  if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
+  p.HC = static_cast<int>((H + chunks - 1) / chunks);
+  p.hchunks = static_cast<int>((H + p.HC - 1) / p.HC);
+  const int64_t items = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), p.hchunks, esz);
+  int64_t ctas = std::min<int64_t>(items, resident);
+  if (sched && sched->ctas > 0) ctas = std::min<int64_t>(ctas, sched->ctas);
+  if (every > 0) {
+    if (partials_override) {
+      if (ctas > partials_cap)
+        return fail(PSKEL_ERR_UNSUPPORTED, "residual scratch of %lld partials exceeds the fixed capacity %lld",
+                    (long long)ctas, (long long)partials_cap);
+      p.partials = partials_override;
+    } else {
+      if (pskel_status q = ensure_buffer(c->partials, static_cast<size_t>(ctas) * sizeof(double))) return q;
+      p.partials = static_cast<double*>(c->partials.ptr);
+    }
+  }
+  // the grid as 32-bit words: a 16-byte vector is 4 words for either dtype
+  CUtensorMap maps[2];
+  const uint64_t dims[3] = {static_cast<uint64_t>(D) * esz / 4, static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
+  const uint64_t strides[2] = {static_cast<uint64_t>(D) * esz, static_cast<uint64_t>(D) * esz * W};
+  const uint32_t box[3] = {136, 18, 1};
+  cudaError_t e = encode_tmap(&maps[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, in, dims, strides, box);
+  if (e == cudaSuccess) e = encode_tmap(&maps[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, out, dims, strides, box);
+  if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled (3D planes)");
+  for (int64_t k = 0; k < iters; ++k) {
+    const bool fwd = (k % 2 == 0);
+    p.src = fwd ? in : out;
+    p.dst = fwd ? out : in;
+    p.steps = 1;
+    p.step0 = k;
+    e = stream3d_tma_step(dtype, &maps[fwd ? 0 : 1], p, static_cast<int>(ctas), s);
+    if (e != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
+  }
+  return PSKEL_OK;
+}
+
 // One step per launch with the streaming kernel (no temporal blocking).
 static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
                              int64_t iters, int R, const pskel_schedule* sched, int64_t every, double* residuals,
@@ -562,18 +613,18 @@ static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64
   p.every = static_cast<int>(every);
   p.residuals = residuals;
   const size_t esz = dtype_size(st.dtype);
-  const bool cross7 = stream3d_is_cross7(st.mask.offsets, st.mask.size, D) &&
-                      (reinterpret_cast<uintptr_t>(in) % (4 * esz)) == 0 &&
-                      (reinterpret_cast<uintptr_t>(out) % (4 * esz)) == 0;
+  const bool cross7 = stream3d_is_cross7(st.mask.offsets, st.mask.size, D, static_cast<int>(esz)) &&
+                      (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0;
+  if (cross7) return stream3d_cross7(st, p, in, out, W, H, D, iters, sched, every, partials_override, partials_cap, c, s);
   // h chunks: a few blocks per SM slot, each marching at least 16 planes
-  const int64_t cols = (cross7 ? (D + 127) / 128 : (D + 31) / 32) * (cross7 ? (W + 15) / 16 : (W + 7) / 8);
+  const int64_t cols = stream3d_ctas(static_cast<int>(W), static_cast<int>(D), 1, cross7, static_cast<int>(esz));
   int64_t chunks = std::max<int64_t>(1, (static_cast<int64_t>(32) * c->sms + cols - 1) / cols);
   chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / 16));
   if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
   p.HC = static_cast<int>((H + chunks - 1) / chunks);
   p.hchunks = static_cast<int>((H + p.HC - 1) / p.HC);
   if (every > 0) {
-    const int64_t need = stream3d_ctas(p.W, p.D, p.hchunks, cross7);
+    const int64_t need = stream3d_ctas(p.W, p.D, p.hchunks, cross7, static_cast<int>(esz));
     if (partials_override) {
       if (need > partials_cap)
         return fail(PSKEL_ERR_UNSUPPORTED, "residual scratch of %lld partials exceeds the fixed capacity %lld",

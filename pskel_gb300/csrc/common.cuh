@@ -83,6 +83,31 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// Sum of squared differences sum((a_i - b_i)^2) over fp32 pairs in
+// double-float arithmetic, so the fp64 pipe (slow on this part) is used once
+// per thread instead of per cell. Error-free transformations: the difference
+// is split exactly into hi + lo (Knuth's TwoSum), hi^2 exactly into p + e
+// (FMA), and p is added to the running (s, c) pair with TwoSum; the 2*hi*lo
+// term and the pair's low part are added in fp32. Relative error of the sum is
+// about 2^-44 -- fp64 accumulation of exact differences gives 2^-53 per add.
+struct SqDiffAcc {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float hi = __fsub_rn(a, b);
+    const float bp = __fsub_rn(hi, a);  // about -b
+    const float ap = __fsub_rn(hi, bp);  // about a
+    const float lo = __fsub_rn(__fsub_rn(a, ap), __fadd_rn(b, bp));
+    const float p = __fmul_rn(hi, hi);
+    const float e = __fmaf_rn(hi, hi, -p);
+    const float t = __fadd_rn(s, p);
+    const float tb = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, tb)), __fsub_rn(p, tb));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, __fadd_rn(e, __fmul_rn(__fmul_rn(2.0f, hi), lo))));
+  }
+  __device__ __forceinline__ double value() const { return static_cast<double>(s) + static_cast<double>(c); }
+};
+
 // Storage conversions. fp32 storage is the identity; bf16 storage widens on
 // load and rounds to nearest even on store.
 template <class TS> struct Storage;

@@ -132,10 +132,20 @@ int stencil3d_max_ctas_per_sm(size_t smem);
 // 32 (d) x 8 (w) columns and h chunk of p.HC planes; residual partials, when
 // the step is reported, go to p.partials[one per block].
 // cross7: the 7-point cross in (centre, h-1, h+1, w-1, w+1, d-1, d+1) order
-// with D % 4 == 0 takes the vectorised variant (a block per 128 d x 8 w).
-bool stream3d_is_cross7(const int* offsets, int n, int64_t D);
-int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7);
+// with D a multiple of the 16-byte vector (4 fp32 / 8 bf16 cells) takes the
+// vectorised variant (a block per 32 vectors of d x 16 w).
+bool stream3d_is_cross7(const int* offsets, int n, int64_t D, int esize);
+int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7, int esize);
 cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, bool cross7, cudaStream_t s);
+// The 7-point cross with TMA-staged planes (persistent blocks over work items
+// of 32 vectors of d x 16 w x p.HC planes); `map` is a 3D tensor map of the
+// source viewed as 32-bit words (dims D*esize/4, W, H; box 136 words x 18
+// rows x 1 plane). Residual partials: one per block.
+size_t stream3d_tma_smem_bytes();
+int stream3d_tma_blocks_per_sm(int dtype);
+int64_t stream3d_tma_items(int W, int D, int hchunks, int esize);
+cudaError_t stream3d_tma_step(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas,
+                              cudaStream_t s);
 cudaError_t stencil3d_pass(int dtype, bool use_tma, const CUtensorMap* map_src, const Stencil3DParams& p, int ctas,
                            cudaStream_t s);
 

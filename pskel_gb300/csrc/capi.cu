@@ -613,18 +613,23 @@ static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64
   p.every = static_cast<int>(every);
   p.residuals = residuals;
   const size_t esz = dtype_size(st.dtype);
-  const bool cross7 = stream3d_is_cross7(st.mask.offsets, st.mask.size, D, static_cast<int>(esz)) &&
+  // the staged kernel holds halo values in storage format: a bf16 grid needs
+  // a halo value that bf16 represents exactly
+  uint32_t hb;
+  std::memcpy(&hb, &st.mask.halo_value, sizeof(hb));
+  const bool halo_exact = st.dtype != PSKEL_BF16 || (hb & 0xFFFFu) == 0u;
+  const bool cross7 = stream3d_is_cross7(st.mask.offsets, st.mask.size, D, static_cast<int>(esz)) && halo_exact &&
                       (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0;
   if (cross7) return stream3d_cross7(st, p, in, out, W, H, D, iters, sched, every, partials_override, partials_cap, c, s);
   // h chunks: a few blocks per SM slot, each marching at least 16 planes
-  const int64_t cols = stream3d_ctas(static_cast<int>(W), static_cast<int>(D), 1, cross7, static_cast<int>(esz));
+  const int64_t cols = stream3d_ctas(static_cast<int>(W), static_cast<int>(D), 1);
   int64_t chunks = std::max<int64_t>(1, (static_cast<int64_t>(32) * c->sms + cols - 1) / cols);
   chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / 16));
   if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
   p.HC = static_cast<int>((H + chunks - 1) / chunks);
   p.hchunks = static_cast<int>((H + p.HC - 1) / p.HC);
   if (every > 0) {
-    const int64_t need = stream3d_ctas(p.W, p.D, p.hchunks, cross7, static_cast<int>(esz));
+    const int64_t need = stream3d_ctas(p.W, p.D, p.hchunks);
     if (partials_override) {
       if (need > partials_cap)
         return fail(PSKEL_ERR_UNSUPPORTED, "residual scratch of %lld partials exceeds the fixed capacity %lld",
@@ -641,7 +646,7 @@ static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64
     p.dst = fwd ? out : in;
     p.steps = 1;
     p.step0 = k;
-    cudaError_t e = stream3d_step(static_cast<int>(st.dtype), p, cross7, s);
+    cudaError_t e = stream3d_step(static_cast<int>(st.dtype), p, s);
     if (e != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
   }
   return PSKEL_OK;

@@ -128,15 +128,14 @@ struct Stencil3DParams {
 
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize);
 int stencil3d_max_ctas_per_sm(size_t smem);
-// One step of the streaming (not temporally blocked) kernel: a block per
-// 32 (d) x 8 (w) columns and h chunk of p.HC planes; residual partials, when
-// the step is reported, go to p.partials[one per block].
-// cross7: the 7-point cross in (centre, h-1, h+1, w-1, w+1, d-1, d+1) order
-// with D a multiple of the 16-byte vector (4 fp32 / 8 bf16 cells) takes the
-// vectorised variant (a block per 32 vectors of d x 16 w).
+// One step of the generic streaming (not temporally blocked) kernel: a block
+// per 32 (d) x 8 (w) columns and h chunk of p.HC planes; residual partials,
+// when the step is reported, go to p.partials[one per block].
+int64_t stream3d_ctas(int W, int D, int hchunks);
+cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, cudaStream_t s);
+// The 7-point cross in (centre, h-1, h+1, w-1, w+1, d-1, d+1) order with D a
+// multiple of the 16-byte vector (4 fp32 / 8 bf16 cells).
 bool stream3d_is_cross7(const int* offsets, int n, int64_t D, int esize);
-int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7, int esize);
-cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, bool cross7, cudaStream_t s);
 // The 7-point cross with TMA-staged planes (persistent blocks over work items
 // of 32 vectors of d x 16 w x p.HC planes); `map` is a 3D tensor map of the
 // source viewed as 32-bit words (dims D*esize/4, W, H; box 136 words x 18

@@ -21,6 +21,7 @@
 // then adds the partials of each reported step in a fixed order, so the norm
 // does not depend on thread timing.
 #include <algorithm>
+#include <cstring>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -326,16 +327,8 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// The 7-point cross (centre, h-1, h+1, w-1, w+1, d-1, d+1, summed in that
-// order) without temporal blocking, vectorised: each thread owns one 16-byte
-// vector of d cells (4 fp32 or 8 bf16, kept packed in registers) in each of
-// two adjacent w rows and marches along h keeping the planes of its cells in
-// registers. Loads run one plane ahead of the arithmetic: while plane h is
-// computed, plane h+2 of the thread's rows, the w-neighbour rows of plane h+1
-// and the d-edge values of plane h+1 (lanes 0 and 31; the other lanes get the
-// d-1 / d+V neighbours from their neighbours by shuffles) are in flight. Four
-// plane slots and two neighbour slots rotate through a four-way unrolled
-// march, so no values move between registers. Requires D % V == 0.
+// 16 bytes of cells (4 fp32 or 8 bf16) kept packed in four 32-bit registers,
+// widened to fp32 on use.
 template <class TS>
 struct Vec16 {
   static constexpr int V = 16 / sizeof(TS);  // cells per vector
@@ -357,186 +350,97 @@ struct Vec16 {
   __device__ __forceinline__ void fill(uint32_t h) { r[0] = r[1] = r[2] = r[3] = h; }
 };
 
-template <class TS, bool kReport>
-__global__ void __launch_bounds__(256, 3) stream3d_cross7_kernel(const __grid_constant__ Stencil3DParams p) {
-  using S = Storage<TS>;
-  using Vt = Vec16<TS>;
-  constexpr int V = Vt::V;
-  __shared__ double s_part[8];
-  // the weights (p.wt) stay in the parameter bank: instruction operands, no registers
-  const TS* __restrict__ src = static_cast<const TS*>(p.src);
-  TS* __restrict__ dst = static_cast<TS*>(p.dst);
-  const float halo = p.halo;
-  // the halo value as raw storage bits (packed twice for bf16)
-  uint32_t hraw;
-  if constexpr (sizeof(TS) == 4) {
-    hraw = __float_as_uint(halo);
-  } else {
-    const uint32_t hb = __bfloat16_as_ushort(__float2bfloat16_rn(halo));
-    hraw = hb | (hb << 16);
-  }
-  const int lane = threadIdx.x & 31;
-  const int d = (blockIdx.x * 32 + lane) * V;
-  const int w = blockIdx.y * 16 + (threadIdx.x >> 5) * 2;
-  const int h0 = blockIdx.z * p.HC;
-  const int h1 = min(p.H, h0 + p.HC);
-  const int H = p.H, D = p.D;
-  const bool d_ok = d < D;
-  const bool row0 = d_ok && w < p.W, row1 = d_ok && w + 1 < p.W;
-  const bool wm_ok = row0 && w > 0, wp_ok = row1 && w + 2 < p.W;
-  const bool el_ok = lane == 0 && d > 0, er_ok = lane == 31 && d + V < D;
-  const int64_t plane = static_cast<int64_t>(p.W) * D;
-  constexpr bool report = kReport;  // this launch's step is a reported one
-  SqDiffAcc acc_res;
-  const int64_t col = static_cast<int64_t>(w) * D + d;
-
-  // loads of plane q: the thread's two rows, the outer w neighbours, the d edges
-  auto ld_rows = [&](int q, Vt (&r)[2]) {
-    const bool in = q >= 0 && q < H;
-    const TS* at = src + (col + q * plane);
-    if (in && row0) r[0].load(at); else r[0].fill(hraw);
-    if (in && row1) r[1].load(at + D); else r[1].fill(hraw);
-  };
-  auto ld_side = [&](int q, Vt (&r)[2], float (&e)[2][2]) {
-    const bool in = q >= 0 && q < H;
-    const TS* at = src + (col + q * plane);
-    if (in && wm_ok) r[0].load(at - D); else r[0].fill(hraw);
-    if (in && wp_ok) r[1].load(at + 2 * D); else r[1].fill(hraw);
-    e[0][0] = (in && el_ok && row0) ? S::load(at[-1]) : halo;
-    e[1][0] = (in && el_ok && row1) ? S::load(at[D - 1]) : halo;
-    e[0][1] = (in && er_ok && row0) ? S::load(at[V]) : halo;
-    e[1][1] = (in && er_ok && row1) ? S::load(at[D + V]) : halo;
-  };
-  // one plane: prefetch h+2 / h+1, then compute plane h from dn, cur, up
-  auto step = [&](int h, Vt (&dn)[2], Vt (&cur)[2], Vt (&up)[2], Vt (&nx)[2], Vt (&sc)[2], Vt (&sn)[2],
-                  float (&ec)[2][2], float (&en)[2][2]) {
-    ld_rows(h + 2, nx);
-    ld_side(h + 1, sn, en);
-    TS* out = dst + (col + h * plane);
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      // every lane takes part in the shuffles; lanes past D hold the halo value
-      float dl = __shfl_up_sync(0xFFFFFFFFu, cur[j].at(V - 1), 1);
-      float dr = __shfl_down_sync(0xFFFFFFFFu, cur[j].at(0), 1);
-      if (lane == 0) dl = ec[j][0];
-      if (lane == 31) dr = ec[j][1];
-      const Vt& wm = (j == 0) ? sc[0] : cur[0];
-      const Vt& wp = (j == 0) ? cur[1] : sc[1];
-      const bool row_ok = (j == 0) ? row0 : row1;
-      // four cells at a time; results are packed to storage as they come
-      uint32_t o[4];
-#pragma unroll
-      for (int g = 0; g < V / 4; ++g) {
-        float res[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int c = 4 * g + k;
-          const float l = (c == 0) ? dl : cur[j].at(c - 1);
-          const float r = (c == V - 1) ? dr : cur[j].at(c + 1);
-          float acc = __fmul_rn(p.wt[0], cur[j].at(c));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[1], dn[j].at(c)));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[2], up[j].at(c)));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[3], wm.at(c)));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[4], wp.at(c)));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[5], l));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[6], r));
-          res[k] = acc;
-        }
-        float stored[4];
-        if constexpr (sizeof(TS) == 4) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            o[k] = __float_as_uint(res[k]);
-            stored[k] = res[k];
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            const __nv_bfloat162 b = __floats2bfloat162_rn(res[2 * k], res[2 * k + 1]);
-            o[2 * g + k] = *reinterpret_cast<const uint32_t*>(&b);
-            stored[2 * k] = __uint_as_float(o[2 * g + k] << 16);
-            stored[2 * k + 1] = __uint_as_float(o[2 * g + k] & 0xFFFF0000u);
-          }
-        }
-        if (report && row_ok) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) acc_res.add(stored[k], cur[j].at(4 * g + k));
-        }
-      }
-      if (row_ok) *reinterpret_cast<uint4*>(out + j * D) = make_uint4(o[0], o[1], o[2], o[3]);
-    }
-  };
-
-  Vt A[2], B[2], C[2], E[2], sA[2], sB[2];
-  float eA[2][2], eB[2][2];
-  ld_rows(h0 - 1, A);
-  ld_rows(h0, B);
-  ld_rows(h0 + 1, C);
-  ld_side(h0, sA, eA);
-  for (int h = h0; h < h1; h += 4) {
-    step(h, A, B, C, E, sA, sB, eA, eB);
-    if (h + 1 >= h1) break;
-    step(h + 1, B, C, E, A, sB, sA, eB, eA);
-    if (h + 2 >= h1) break;
-    step(h + 2, C, E, A, B, sA, sB, eA, eB);
-    if (h + 3 >= h1) break;
-    step(h + 3, E, A, B, C, sB, sA, eB, eA);
-  }
-  if constexpr (kReport) {
-    double v = acc_res.value();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-    if (lane == 0) s_part[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int i = 0; i < 8; ++i) t += s_part[i];
-      const int cta = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-      p.partials[cta] = t;
-    }
-  }
-}
-
-// The same 7-point cross, one step per launch, with the planes staged in
-// shared memory by TMA. A persistent block owns a work item of 32 vectors of
-// d (128 fp32 / 256 bf16 cells) x 16 w rows x p.HC planes; one 3D TMA copy
-// per plane brings the 34-vector x 18-row box (one vector and one row of
-// halo on each side) into a ring of kS3Slots plane slots. The producer
-// (thread 0) runs up to three planes ahead of the plane being computed and
-// across work items; each slot has an mbarrier, and a slot is reused only
-// after the block barrier that follows its last read. Out-of-grid positions
-// (zero-filled by TMA) are replaced by the mask halo value.
+// The 7-point cross (centre, h-1, h+1, w-1, w+1, d-1, d+1, summed in that
+// order), one step per launch, with the planes staged in shared memory by TMA.
+// A persistent block owns work items of 32 vectors of d (128 fp32 / 256 bf16
+// cells) x 16 w rows x p.HC planes. A producer warp streams the planes h0-1 ..
+// h1 of its items, one 3D TMA copy per plane of the 34-vector x 18-row box
+// (a vector and a row of halo on each side; positions outside the grid are
+// zero-filled), into a ring of kS3Slots slots. Each slot has a "full"
+// mbarrier (the copy landed) and an "empty" one (all eight consumer warps
+// have read it), so consumer warps run independently of each other, up to
+// the ring's depth. Every wait is bounded. With a zero halo value the zero
+// fill is the halo; otherwise out-of-grid positions are replaced by it.
 constexpr int kS3Slots = 6;
 constexpr int kS3BoxX = 34;                 // 16-byte vectors per staged row
 constexpr int kS3RowBytes = kS3BoxX * 16;   // 544
 constexpr int kS3BoxY = 18;                 // 16 rows + one each side
 constexpr int kS3PlaneBytes = (kS3RowBytes * kS3BoxY + 127) & ~127;
-constexpr int kS3Threads = 256;
+constexpr int kS3Consumers = 8;             // consumer warps, two w rows each
+constexpr int kS3Threads = 32 * (kS3Consumers + 1);
 
-template <class TS, bool kReport>
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// barrier among the consumer warps only (the producer warp may have left)
+__device__ __forceinline__ void consumers_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(32 * kS3Consumers) : "memory");
+}
+
+template <class TS, bool kReport, bool kZeroHalo>
 __global__ void __launch_bounds__(kS3Threads, 3)
     stream3d_tma_kernel(const __grid_constant__ CUtensorMap map, const __grid_constant__ Stencil3DParams p) {
   using S = Storage<TS>;
   using Vt = Vec16<TS>;
   constexpr int V = Vt::V;
   extern __shared__ __align__(128) uint8_t smem_raw[];
-  __shared__ double s_part[kS3Threads / 32];
+  __shared__ double s_part[kS3Consumers];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if ((smem_u32(smem_raw) & 127u) != 0) {
     if (tid == 0) atomicOr(p.err, kDevErrAlign);
     return;
   }
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + kS3Slots * kS3PlaneBytes);
+  uint64_t* empty = full + kS3Slots;
   if (tid == 0) {
-    for (int i = 0; i < kS3Slots; ++i) mbar_init(&full[i], 1);
+    for (int i = 0; i < kS3Slots; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kS3Consumers);
+    }
     fence_barrier_init();
-    prefetch_tensormap(&map);
   }
   __syncthreads();
 
   const int H = p.H, W = p.W, D = p.D;
   const int dblocks = (D + 32 * V - 1) / (32 * V), wblocks = (W + 15) / 16;
   const int64_t items = static_cast<int64_t>(dblocks) * wblocks * p.hchunks;
+  auto geometry = [&](int64_t it, int& d0, int& w0, int& h0, int& h1) {
+    const int db = static_cast<int>(it % dblocks);
+    const int64_t r = it / dblocks;
+    d0 = db * 32 * V;
+    w0 = static_cast<int>(r % wblocks) * 16;
+    h0 = static_cast<int>(r / wblocks) * p.HC;
+    h1 = min(H, h0 + p.HC);
+  };
+
+  if (warp == kS3Consumers) {
+    // ---- producer: planes h0-1 .. h1 of every item, in order
+    if (lane == 0) {
+      prefetch_tensormap(&map);
+      int slot = 0;
+      uint32_t use = 0;
+      for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+        int d0, w0, h0, h1;
+        geometry(it, d0, w0, h0, h1);
+        // the map addresses the grid as 32-bit words (a box row of 136 words)
+        const int x = (d0 - V) * static_cast<int>(sizeof(TS)) / 4;
+        for (int q = h0 - 1; q <= h1; ++q) {
+          if (use > 0 && !mbar_wait_bounded(&empty[slot], (use - 1) & 1u, p.err)) return;
+          fence_proxy_async();
+          mbar_arrive_expect_tx(&full[slot], static_cast<uint32_t>(kS3RowBytes * kS3BoxY));
+          tma_load_3d(smem_raw + slot * kS3PlaneBytes, &map, x, w0 - 1, q, &full[slot]);
+          if (++slot == kS3Slots) {
+            slot = 0;
+            ++use;
+          }
+        }
+      }
+    }
+    return;
+  }
+
+  // ---- consumers
   const int64_t plane = static_cast<int64_t>(W) * D;
   TS* __restrict__ dst = static_cast<TS*>(p.dst);
   const float halo = p.halo;
@@ -547,122 +451,103 @@ __global__ void __launch_bounds__(kS3Threads, 3)
     const uint32_t hb = __bfloat16_as_ushort(__float2bfloat16_rn(halo));
     hraw = hb | (hb << 16);
   }
+  // this thread's staged rows: row 0 of the box is w0-1
+  const int r0 = 2 * warp + 1;
+  const uint8_t* const sbase = smem_raw;
+  const int o_row0 = r0 * kS3RowBytes + (lane + 1) * 16;
+  const int o_el = r0 * kS3RowBytes + (V - 1) * static_cast<int>(sizeof(TS));  // d0-1
+  const int o_er = r0 * kS3RowBytes + 33 * 16;                                  // d0+32V
   SqDiffAcc acc_res;
-
-  // in-grid planes of an item: qlo .. qhi (planes h0-1 .. h1 clipped to the grid)
-  auto item_planes = [&](int64_t it, int& d0, int& w0, int& h0, int& h1, int& qlo, int& qhi) {
-    const int db = static_cast<int>(it % dblocks);
-    const int64_t r = it / dblocks;
-    const int wb = static_cast<int>(r % wblocks);
-    const int ch = static_cast<int>(r / wblocks);
-    d0 = db * 32 * V;
-    w0 = wb * 16;
-    h0 = ch * p.HC;
-    h1 = min(H, h0 + p.HC);
-    qlo = max(h0 - 1, 0);
-    qhi = min(h1, H - 1);
+  auto ld = [&](int slot, int off, Vt& v) {
+    const uint4 x = *reinterpret_cast<const uint4*>(sbase + slot * kS3PlaneBytes + off);
+    v.r[0] = x.x;
+    v.r[1] = x.y;
+    v.r[2] = x.z;
+    v.r[3] = x.w;
   };
-
-  // producer state (thread 0): the next plane to issue and the sequence count
-  int64_t p_item = blockIdx.x;
-  int p_q = 0, p_qhi = -1, p_d0 = 0, p_w0 = 0;
-  uint32_t issued = 0;
-  auto p_load_item = [&]() {
-    int h0, h1;
-    if (p_item < items) item_planes(p_item, p_d0, p_w0, h0, h1, p_q, p_qhi);
+  auto ld1 = [&](int slot, int off) -> float {
+    return S::load(*reinterpret_cast<const TS*>(sbase + slot * kS3PlaneBytes + off));
   };
-  auto produce_upto = [&](uint32_t limit) {
-    while (issued < limit && p_item < items) {
-      const int slot = static_cast<int>(issued % kS3Slots);
-      fence_proxy_async();
-      mbar_arrive_expect_tx(&full[slot], static_cast<uint32_t>(kS3RowBytes * kS3BoxY));
-      // the map addresses the grid as 32-bit words (a box row of 136 words)
-      tma_load_3d(smem_raw + slot * kS3PlaneBytes, &map, (p_d0 - V) * static_cast<int>(sizeof(TS)) / 4, p_w0 - 1,
-                  p_q, &full[slot]);
-      ++issued;
-      if (++p_q > p_qhi) {
-        p_item += gridDim.x;
-        p_load_item();
-      }
-    }
-  };
-  if (tid == 0) {
-    p_load_item();
-    produce_upto(kS3Slots);
-  }
+  auto next = [](int s) { return s + 1 == kS3Slots ? 0 : s + 1; };
+  bool alive = true;
+  // slot and phase parity of the next plane in the sequence
+  int s_next = 0;
+  uint32_t ph_next = 0;
+  auto wait_full = [&](int slot, uint32_t ph) -> bool { return mbar_wait_bounded(&full[slot], ph, p.err); };
 
-  uint32_t seq_base = 0;  // sequence number of the current item's plane qlo
-  bool ok_all = true;
-  for (int64_t it = blockIdx.x; it < items && ok_all; it += gridDim.x) {
-    int d0, w0, h0, h1, qlo, qhi;
-    item_planes(it, d0, w0, h0, h1, qlo, qhi);
+  for (int64_t it = blockIdx.x; it < items && alive; it += gridDim.x) {
+    int d0, w0, h0, h1;
+    geometry(it, d0, w0, h0, h1);
     const int d = d0 + lane * V;
     const int w = w0 + warp * 2;
     const bool d_ok = d < D;
     const bool row0 = d_ok && w < W, row1 = d_ok && w + 1 < W;
-    const bool wm_ok = row0 && w > 0, wp_ok = row1 && w + 2 < W;
-    const bool el_ok = lane == 0 && d > 0, er_ok = lane == 31 && d + V < D;
-    auto seq_of = [&](int q) { return seq_base + static_cast<uint32_t>(q - qlo); };
-    auto in_grid = [&](int q) { return q >= 0 && q < H; };
-    // wait (thread 0) for plane q, publish to the block with the barrier
-    auto wait_plane = [&](int q) -> bool {
-      int ok = 1;
-      if (tid == 0 && in_grid(q)) {
-        const uint32_t k = seq_of(q);
-        ok = mbar_wait_bounded(&full[k % kS3Slots], (k / kS3Slots) & 1u, p.err) ? 1 : 0;
-      }
-      return __syncthreads_and(ok) != 0;
-    };
-    auto row_ptr = [&](int q, int r) -> const uint8_t* {
-      return smem_raw + (seq_of(q) % kS3Slots) * kS3PlaneBytes + r * kS3RowBytes;
-    };
-    auto rd = [&](int q, int r, bool ok, Vt& v) {
-      if (ok && in_grid(q)) {
-        const uint4 x = *reinterpret_cast<const uint4*>(row_ptr(q, r) + (lane + 1) * 16);
-        v.r[0] = x.x;
-        v.r[1] = x.y;
-        v.r[2] = x.z;
-        v.r[3] = x.w;
-      } else {
-        v.fill(hraw);
-      }
-    };
-    auto rd_edge = [&](int q, int r, bool ok, int vec, int c) -> float {
-      if (!(ok && in_grid(q))) return halo;
-      const TS* e = reinterpret_cast<const TS*>(row_ptr(q, r) + vec * 16);
-      return S::load(e[c]);
-    };
-
-    if (!wait_plane(h0 - 1) || !wait_plane(h0)) {
-      ok_all = false;
+    // general halo: which staged values lie outside the grid
+    const bool wm_in = row0 && w > 0, wp_in = row1 && w + 2 < W;
+    const bool el_in = d0 > 0, er_in = d0 + 32 * V < D;
+    int s_dn = s_next, s_cur = next(s_dn), s_up = next(s_cur);
+    uint32_t ph_dn = ph_next, ph_cur = ph_next ^ (s_cur == 0 ? 1u : 0u), ph_up = ph_cur ^ (s_up == 0 ? 1u : 0u);
+    if (!wait_full(s_dn, ph_dn) || !wait_full(s_cur, ph_cur)) {
+      alive = false;
       break;
     }
-    const int r0 = 2 * warp + 1;  // staged row of the thread's first w row
     for (int h = h0; h < h1; ++h) {
-      if (!wait_plane(h + 1)) {
-        ok_all = false;
+      if (!wait_full(s_up, ph_up)) {
+        alive = false;
         break;
       }
-      // planes below h-1 are no longer read: their slots may be refilled
-      if (tid == 0) produce_upto(seq_of(max(h - 1, qlo)) + kS3Slots);
       Vt dn[2], cur[2], up[2], wm, wp;
-      rd(h - 1, r0, row0, dn[0]);
-      rd(h - 1, r0 + 1, row1, dn[1]);
-      rd(h, r0, row0, cur[0]);
-      rd(h, r0 + 1, row1, cur[1]);
-      rd(h + 1, r0, row0, up[0]);
-      rd(h + 1, r0 + 1, row1, up[1]);
-      rd(h, r0 - 1, wm_ok, wm);
-      rd(h, r0 + 2, wp_ok, wp);
-      const float el0 = rd_edge(h, r0, el_ok && row0, 0, V - 1), el1 = rd_edge(h, r0 + 1, el_ok && row1, 0, V - 1);
-      const float er0 = rd_edge(h, r0, er_ok && row0, 33, 0), er1 = rd_edge(h, r0 + 1, er_ok && row1, 33, 0);
+      ld(s_dn, o_row0, dn[0]);
+      ld(s_dn, o_row0 + kS3RowBytes, dn[1]);
+      ld(s_cur, o_row0, cur[0]);
+      ld(s_cur, o_row0 + kS3RowBytes, cur[1]);
+      ld(s_up, o_row0, up[0]);
+      ld(s_up, o_row0 + kS3RowBytes, up[1]);
+      ld(s_cur, o_row0 - kS3RowBytes, wm);
+      ld(s_cur, o_row0 + 2 * kS3RowBytes, wp);
+      float el[2] = {0.0f, 0.0f}, er[2] = {0.0f, 0.0f};
+      if (lane == 0) {
+        el[0] = ld1(s_cur, o_el);
+        el[1] = ld1(s_cur, o_el + kS3RowBytes);
+      }
+      if (lane == 31) {
+        er[0] = ld1(s_cur, o_er);
+        er[1] = ld1(s_cur, o_er + kS3RowBytes);
+      }
+      // plane h-1 is read for the last time
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s_dn]);
+      if constexpr (!kZeroHalo) {
+        if (h - 1 < 0) {
+          dn[0].fill(hraw);
+          dn[1].fill(hraw);
+        }
+        if (h + 1 >= H) {
+          up[0].fill(hraw);
+          up[1].fill(hraw);
+        }
+        if (!row0) {
+          dn[0].fill(hraw);
+          cur[0].fill(hraw);
+          up[0].fill(hraw);
+        }
+        if (!row1) {
+          dn[1].fill(hraw);
+          cur[1].fill(hraw);
+          up[1].fill(hraw);
+        }
+        if (!wm_in) wm.fill(hraw);
+        if (!wp_in) wp.fill(hraw);
+        if (!el_in) el[0] = el[1] = halo;
+        if (!er_in) er[0] = er[1] = halo;
+      }
       TS* out = dst + (h * plane + static_cast<int64_t>(w) * D + d);
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         float dl = __shfl_up_sync(0xFFFFFFFFu, cur[j].at(V - 1), 1);
         float dr = __shfl_down_sync(0xFFFFFFFFu, cur[j].at(0), 1);
-        if (lane == 0) dl = (j == 0) ? el0 : el1;
-        if (lane == 31) dr = (j == 0) ? er0 : er1;
+        if (lane == 0) dl = el[j];
+        if (lane == 31) dr = er[j];
         const Vt& a = (j == 0) ? wm : cur[0];
         const Vt& b = (j == 0) ? cur[1] : wp;
         const bool row_ok = (j == 0) ? row0 : row1;
@@ -707,22 +592,32 @@ __global__ void __launch_bounds__(kS3Threads, 3)
         }
         if (row_ok) *reinterpret_cast<uint4*>(out + j * D) = make_uint4(o[0], o[1], o[2], o[3]);
       }
+      s_dn = s_cur;
+      ph_dn = ph_cur;
+      s_cur = s_up;
+      ph_cur = ph_up;
+      s_up = next(s_up);
+      ph_up ^= (s_up == 0) ? 1u : 0u;
     }
-    if (!ok_all) break;
-    // every plane of the item has been read once the block passes this barrier
-    __syncthreads();
-    seq_base += static_cast<uint32_t>(qhi - qlo + 1);
-    if (tid == 0) produce_upto(seq_base + kS3Slots);
+    if (!alive) break;
+    // planes h1-1 and h1 are released at the end of the item
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(&empty[s_dn]);
+      mbar_arrive(&empty[s_cur]);
+    }
+    s_next = s_up;
+    ph_next = ph_up;
   }
   if constexpr (kReport) {
     double v = acc_res.value();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
     if (lane == 0) s_part[warp] = v;
-    __syncthreads();
+    consumers_sync();
     if (tid == 0) {
       double t = 0.0;
-      for (int i = 0; i < kS3Threads / 32; ++i) t += s_part[i];
+      for (int i = 0; i < kS3Consumers; ++i) t += s_part[i];
       p.partials[blockIdx.x] = t;
     }
   }
@@ -764,17 +659,9 @@ cudaError_t launch3d(const CUtensorMap* map, const Stencil3DParams& p, int ctas,
 }
 
 template <class TS, int NM>
-cudaError_t launch_stream(const Stencil3DParams& p, bool cross7, cudaStream_t s) {
-  constexpr int kD = 32 * (16 / static_cast<int>(sizeof(TS)));  // d cells per cross7 block
-  const dim3 grid(cross7 ? (p.D + kD - 1) / kD : (p.D + 31) / 32, cross7 ? (p.W + 15) / 16 : (p.W + 7) / 8,
-                  p.hchunks);
-  const bool report = p.every > 0 && ((p.step0 + 1) % p.every) == 0;
-  if (cross7 && report)
-    stream3d_cross7_kernel<TS, true><<<grid, 256, 0, s>>>(p);
-  else if (cross7)
-    stream3d_cross7_kernel<TS, false><<<grid, 256, 0, s>>>(p);
-  else
-    stream3d_kernel<TS, NM><<<grid, 256, 0, s>>>(p);
+cudaError_t launch_stream(const Stencil3DParams& p, cudaStream_t s) {
+  const dim3 grid((p.D + 31) / 32, (p.W + 7) / 8, p.hchunks);
+  stream3d_kernel<TS, NM><<<grid, 256, 0, s>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || p.every <= 0 || ((p.step0 + 1) % p.every) != 0) return e;
   const int nctas = static_cast<int>(grid.x * grid.y * grid.z);
@@ -793,24 +680,31 @@ bool stream3d_is_cross7(const int* offsets, int n, int64_t D, int esize) {
   return true;
 }
 
-int64_t stream3d_ctas(int W, int D, int hchunks, bool cross7, int esize) {
-  const int kD = 32 * (16 / esize);
-  return static_cast<int64_t>(cross7 ? (D + kD - 1) / kD : (D + 31) / 32) * (cross7 ? (W + 15) / 16 : (W + 7) / 8) *
-         hchunks;
+int64_t stream3d_ctas(int W, int D, int hchunks) {
+  return static_cast<int64_t>((D + 31) / 32) * ((W + 7) / 8) * hchunks;
 }
 
-size_t stream3d_tma_smem_bytes() { return kS3Slots * kS3PlaneBytes + 8 * kS3Slots; }
+size_t stream3d_tma_smem_bytes() { return kS3Slots * kS3PlaneBytes + 16 * kS3Slots; }
+
+template <class TS>
+int tma_blocks_per_sm() {
+  const size_t smem = stream3d_tma_smem_bytes();
+  void* ks[4] = {reinterpret_cast<void*>(stream3d_tma_kernel<TS, false, false>),
+                 reinterpret_cast<void*>(stream3d_tma_kernel<TS, false, true>),
+                 reinterpret_cast<void*>(stream3d_tma_kernel<TS, true, false>),
+                 reinterpret_cast<void*>(stream3d_tma_kernel<TS, true, true>)};
+  int best = 1 << 30;
+  for (void* k : ks) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kS3Threads, smem) != cudaSuccess) n = 1;
+    best = std::min(best, n);
+  }
+  return std::max(1, best);
+}
 
 int stream3d_tma_blocks_per_sm(int dtype) {
-  const size_t smem = stream3d_tma_smem_bytes();
-  auto k = (dtype == 2) ? stream3d_tma_kernel<__nv_bfloat16, false> : stream3d_tma_kernel<float, false>;
-  auto kr = (dtype == 2) ? stream3d_tma_kernel<__nv_bfloat16, true> : stream3d_tma_kernel<float, true>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  int n = 0, nr = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kS3Threads, smem) != cudaSuccess) n = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nr, kr, kS3Threads, smem) != cudaSuccess) nr = 1;
-  return std::max(1, std::min(n, nr));
+  return dtype == 2 ? tma_blocks_per_sm<__nv_bfloat16>() : tma_blocks_per_sm<float>();
 }
 
 int64_t stream3d_tma_items(int W, int D, int hchunks, int esize) {
@@ -818,31 +712,38 @@ int64_t stream3d_tma_items(int W, int D, int hchunks, int esize) {
   return static_cast<int64_t>((D + kD - 1) / kD) * ((W + 15) / 16) * hchunks;
 }
 
+template <class TS>
+void launch_tma(const CUtensorMap* map, const Stencil3DParams& p, int ctas, bool report, cudaStream_t s) {
+  const size_t smem = stream3d_tma_smem_bytes();
+  uint32_t hbits;
+  std::memcpy(&hbits, &p.halo, sizeof(hbits));
+  const bool zero = hbits == 0u;  // +0.0 exactly: the TMA zero fill is the halo
+  if (report && zero)
+    stream3d_tma_kernel<TS, true, true><<<ctas, kS3Threads, smem, s>>>(*map, p);
+  else if (report)
+    stream3d_tma_kernel<TS, true, false><<<ctas, kS3Threads, smem, s>>>(*map, p);
+  else if (zero)
+    stream3d_tma_kernel<TS, false, true><<<ctas, kS3Threads, smem, s>>>(*map, p);
+  else
+    stream3d_tma_kernel<TS, false, false><<<ctas, kS3Threads, smem, s>>>(*map, p);
+}
+
 cudaError_t stream3d_tma_step(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas,
                               cudaStream_t s) {
   const bool report = p.every > 0 && ((p.step0 + 1) % p.every) == 0;
-  const size_t smem = stream3d_tma_smem_bytes();
-  if (dtype == 2) {
-    if (report)
-      stream3d_tma_kernel<__nv_bfloat16, true><<<ctas, kS3Threads, smem, s>>>(*map, p);
-    else
-      stream3d_tma_kernel<__nv_bfloat16, false><<<ctas, kS3Threads, smem, s>>>(*map, p);
-  } else {
-    if (report)
-      stream3d_tma_kernel<float, true><<<ctas, kS3Threads, smem, s>>>(*map, p);
-    else
-      stream3d_tma_kernel<float, false><<<ctas, kS3Threads, smem, s>>>(*map, p);
-  }
+  if (dtype == 2)
+    launch_tma<__nv_bfloat16>(map, p, ctas, report, s);
+  else
+    launch_tma<float>(map, p, ctas, report, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || !report) return e;
   reduce3d_residual<<<1, 256, 0, s>>>(p.partials, ctas, 1, p.step0, p.every, p.residuals);
   return cudaGetLastError();
 }
 
-cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, bool cross7, cudaStream_t s) {
-  if (dtype == 2)
-    return p.nm == 7 ? launch_stream<__nv_bfloat16, 7>(p, cross7, s) : launch_stream<__nv_bfloat16, 0>(p, cross7, s);
-  return p.nm == 7 ? launch_stream<float, 7>(p, cross7, s) : launch_stream<float, 0>(p, cross7, s);
+cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, cudaStream_t s) {
+  if (dtype == 2) return p.nm == 7 ? launch_stream<__nv_bfloat16, 7>(p, s) : launch_stream<__nv_bfloat16, 0>(p, s);
+  return p.nm == 7 ? launch_stream<float, 7>(p, s) : launch_stream<float, 0>(p, s);
 }
 
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize) {

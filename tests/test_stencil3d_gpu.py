@@ -62,6 +62,24 @@ def test_heat3d_matches_oracle(cuda, oracle_mod, dtype, W, H, D, iters):
     np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
 
 
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H,D", [(40, 33, 72), (17, 50, 264), (300, 7, 8)])
+@pytest.mark.parametrize("th,ctas", [(0, 0), (3, 1), (64, 5), (1, 0)])
+@pytest.mark.parametrize("halo", [0.0, -0.0, 0.1])
+def test_heat3d_streaming_items(cuda, oracle_mod, dtype, W, H, D, th, ctas, halo):
+    # one step per launch (planes staged by TMA): ragged blocks in w and d,
+    # work items of th planes, few persistent blocks (every block runs many
+    # items through its plane ring); +0.0 is the zero-filled halo, -0.0 the
+    # substituted one, 0.1 (not a bf16 value) takes the generic kernel for bf16
+    keep = P._Keep()
+    a, b = grids(W, H, D, W * H + D, dtype)
+    sch = dict(time_steps=1, tile_w=0, tile_h=th, tile_d=0, ctas=ctas)
+    got, res = run3d(cuda, heat(keep, dtype, halo=halo), a, b, 6, sched=sch, every=3, dtype=dtype)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 6, halo=halo, dtype=dtype, every=3)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
+
+
 @pytest.mark.parametrize("T,tw,td,th", [(1, 0, 0, 0), (2, 16, 32, 0), (3, 8, 16, 5), (4, 32, 64, 7), (8, 8, 8, 0),
                                         (2, 0, 0, 1), (3, 16, 16, 13)])
 def test_heat3d_schedules(cuda, oracle_mod, T, tw, td, th):

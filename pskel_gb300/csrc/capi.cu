@@ -318,6 +318,33 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
   p.pitch = pitch;
   p.ring = ring;
   p.R = 1;
+  p.err = c->err;
+  if (advect) {
+    p.K = st.diffusivity;
+    p.dt = st.dt;
+    p.inv_dx = st.inv_dx;
+    p.u = st.wind_u;
+    p.v = st.wind_v;
+  } else {
+    p.nm = st.mask.size;
+    for (int n = 0; n < p.nm; ++n) p.wt[n] = st.mask.weights[n];
+  }
+  if (T == 1) {
+    // one step per pass: the streaming kernel, a warp per 32 vectors of
+    // columns x HC rows (tile_h, default 16)
+    p.TH = (sched && sched->tile_h > 0) ? static_cast<int>(std::min<int64_t>(sched->tile_h, H)) : 16;
+    p.tiles_y = static_cast<int>((H + p.TH - 1) / p.TH);
+    *used = true;
+    for (int64_t k = 0; k < iters; ++k) {
+      const bool fwd = (k % 2 == 0);
+      p.src = fwd ? in : out;
+      p.dst = fwd ? out : in;
+      p.steps = 1;
+      cudaError_t e = stream2d_step(opk, dtype, p, s);
+      if (e != cudaSuccess) return cuda_fail(e, "2D streaming kernel launch");
+    }
+    return PSKEL_OK;
+  }
   p.T = T;
   p.TW = LW - 2 * HX;
   p.TH = LH - 2 * HY;
@@ -327,15 +354,6 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
   p.HY = HY;
   p.tiles_x = static_cast<int>((W + p.TW - 1) / p.TW);
   p.tiles_y = static_cast<int>((H + p.TH - 1) / p.TH);
-  p.err = c->err;
-  if (advect) {
-    p.K = st.diffusivity;
-    p.dt = st.dt;
-    p.inv_dx = st.inv_dx;
-  } else {
-    p.nm = st.mask.size;
-    for (int n = 0; n < p.nm; ++n) p.wt[n] = st.mask.weights[n];
-  }
   const int ntiles = p.tiles_x * p.tiles_y;
   const int per_sm = std::max(1, fast2d_max_ctas_per_sm(advect, dtype, S));
   int ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
@@ -350,10 +368,6 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
   cudaError_t e = encode_tmap(&m_in, tt, 2, in, dims, strides, box);
   if (e == cudaSuccess) e = encode_tmap(&m_out, tt, 2, out, dims, strides, box);
   if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled");
-  if (advect) {
-    p.u = st.wind_u;
-    p.v = st.wind_v;
-  }
   *used = true;
   const std::vector<int> passes = plan_passes(iters, T);
   for (size_t i = 0; i < passes.size(); ++i) {

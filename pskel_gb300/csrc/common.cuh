@@ -120,4 +120,27 @@ template <> struct Storage<__nv_bfloat16> {
   static __device__ __forceinline__ __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
 };
 
+// 16 bytes of cells (4 fp32 or 8 bf16) kept packed in four 32-bit registers,
+// widened to fp32 on use.
+template <class TS>
+struct Vec16 {
+  static constexpr int V = 16 / sizeof(TS);  // cells per vector
+  uint32_t r[4];                             // raw 16 bytes
+  __device__ __forceinline__ float at(int c) const {
+    if constexpr (sizeof(TS) == 4) {
+      return __uint_as_float(r[c]);
+    } else {
+      return (c & 1) ? __uint_as_float(r[c >> 1] & 0xFFFF0000u) : __uint_as_float(r[c >> 1] << 16);
+    }
+  }
+  __device__ __forceinline__ void load(const TS* p) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+    r[0] = v.x;
+    r[1] = v.y;
+    r[2] = v.z;
+    r[3] = v.w;
+  }
+  __device__ __forceinline__ void fill(uint32_t h) { r[0] = r[1] = r[2] = r[3] = h; }
+};
+
 }  // namespace pskel

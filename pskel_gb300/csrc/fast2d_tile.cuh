@@ -91,6 +91,22 @@ __device__ __forceinline__ void ld_wind(const TS* f, int64_t pitch, int gy, int 
   }
 }
 
+// One advection-diffusion update (the reference's CLOUDSIM arithmetic,
+// PSkelStencil.hpp:347-387): centre cc, neighbours north n_ (row above), east
+// e_, west w_, south s_ (row below), winds xw, yw; no contraction.
+__device__ __forceinline__ float advect_cell(float cc, float n_, float e_, float w_, float s_, float xw, float yw,
+                                             float K, float dt, float inv_dx) {
+  const float sum = __fsub_rn(__fmul_rn(4.0f, cc), __fadd_rn(__fadd_rn(__fadd_rn(n_, e_), w_), s_));
+  const float cvy = (yw > 0.0f) ? yw : -yw;  // yf * yw with yf = +-1
+  const float cvx = (xw > 0.0f) ? xw : -xw;
+  const float nbx = (xw > 0.0f) ? e_ : w_;
+  const float nby = (yw > 0.0f) ? s_ : n_;
+  const float temp_wind = __fsub_rn(__fmul_rn(-cvx, __fmul_rn(__fsub_rn(cc, nbx), inv_dx)),
+                                    __fmul_rn(cvy, __fmul_rn(__fsub_rn(cc, nby), inv_dx)));
+  const float cond = __fmul_rn(__fmul_rn(-K, __fmul_rn(sum, 0.25f)), dt);
+  return __fadd_rn(__fadd_rn(cc, cond), __fmul_rn(temp_wind, dt));
+}
+
 // Geometry and op parameters of one tile's grid (passed in registers).
 struct TileGeom {
   int W, H, ring, steps;
@@ -147,23 +163,9 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
         ld_wind(wu, g.pitch, gy0 + y, gxv, g.W, g.H, uu);
         ld_wind(wv, g.pitch, gy0 + y, gxv, g.W, g.H, vv);
 #pragma unroll
-        for (int c = 0; c < N; ++c) {
-          const float cc = win[k][1 + c];
-          const float n_ = win[k - 1][1 + c];
-          const float e_ = win[k][2 + c];
-          const float w_ = win[k][c];
-          const float s_ = win[k + 1][1 + c];
-          const float sum = __fsub_rn(__fmul_rn(4.0f, cc), __fadd_rn(__fadd_rn(__fadd_rn(n_, e_), w_), s_));
-          const float xw = uu[c], yw = vv[c];
-          const float cvy = (yw > 0.0f) ? yw : -yw;  // yf * yw with yf = +-1
-          const float cvx = (xw > 0.0f) ? xw : -xw;
-          const float nbx = (xw > 0.0f) ? e_ : w_;
-          const float nby = (yw > 0.0f) ? s_ : n_;
-          const float temp_wind = __fsub_rn(__fmul_rn(-cvx, __fmul_rn(__fsub_rn(cc, nbx), g.inv_dx)),
-                                            __fmul_rn(cvy, __fmul_rn(__fsub_rn(cc, nby), g.inv_dx)));
-          const float cond = __fmul_rn(__fmul_rn(-g.K, __fmul_rn(sum, 0.25f)), g.dt);
-          res[c] = __fadd_rn(__fadd_rn(cc, cond), __fmul_rn(temp_wind, g.dt));
-        }
+        for (int c = 0; c < N; ++c)
+          res[c] = advect_cell(win[k][1 + c], win[k - 1][1 + c], win[k][2 + c], win[k][c], win[k + 1][1 + c], uu[c],
+                               vv[c], g.K, g.dt, g.inv_dx);
       }
       TS* o = out + y * LW + x0;
       if (ring_tile) {

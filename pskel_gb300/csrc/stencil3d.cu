@@ -327,29 +327,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// 16 bytes of cells (4 fp32 or 8 bf16) kept packed in four 32-bit registers,
-// widened to fp32 on use.
-template <class TS>
-struct Vec16 {
-  static constexpr int V = 16 / sizeof(TS);  // cells per vector
-  uint32_t r[4];                             // raw 16 bytes
-  __device__ __forceinline__ float at(int c) const {
-    if constexpr (sizeof(TS) == 4) {
-      return __uint_as_float(r[c]);
-    } else {
-      return (c & 1) ? __uint_as_float(r[c >> 1] & 0xFFFF0000u) : __uint_as_float(r[c >> 1] << 16);
-    }
-  }
-  __device__ __forceinline__ void load(const TS* p) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-    r[0] = v.x;
-    r[1] = v.y;
-    r[2] = v.z;
-    r[3] = v.w;
-  }
-  __device__ __forceinline__ void fill(uint32_t h) { r[0] = r[1] = r[2] = r[3] = h; }
-};
-
 // The 7-point cross (centre, h-1, h+1, w-1, w+1, d-1, d+1, summed in that
 // order), one step per launch, with the planes staged in shared memory by TMA.
 // A persistent block owns work items of 32 vectors of d (128 fp32 / 256 bf16

@@ -193,6 +193,35 @@ def test_advection_c3_full_size_and_fp64_error(cuda, oracle_mod):
     assert err32 < 1e-4 and errb < 0.1
 
 
+def test_advection_c3_full_size_and_fp64_error(cuda, oracle_mod):
+    # 4096^2, 500 iterations: fp32 and bf16 storage bit-exact against the
+    # oracle; their errors against the fp64 oracle are reported
+    W = H = 4096
+    a, b, u, v = S.advect2d(W, H, seed=1)
+    got = _advect_gpu(cuda, "f32", a, b, u, v, 500)
+    want = oracle_mod.advect(a, b, u, v, 500, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX)
+    assert np.array_equal(bits(got), bits(want))
+    ref64 = oracle_mod.advect(a.astype(np.float64), b.astype(np.float64), u.astype(np.float64),
+                              v.astype(np.float64), 500, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype="f64")
+    ab, bb, ub, vb = (S.f32_to_bf16(x) for x in (a, b, u, v))
+    gb = _advect_gpu(cuda, "bf16", ab, bb, ub, vb, 500)
+    wantb = oracle_mod.advect(ab, bb, ub, vb, 500, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype="bf16")
+    assert np.array_equal(gb, wantb)
+    err32 = float(np.max(np.abs(got - ref64)))
+    # the bf16 run also stores its winds in bf16, and every step rounds the
+    # field to 8 significand bits: an update smaller than half a bf16 ulp of
+    # the cell is lost, so the error grows with the number of steps
+    gbf = S.bf16_to_f32(gb).astype(np.float64)
+    errb = float(np.max(np.abs(gbf - ref64)))
+    relb = float(np.linalg.norm(gbf - ref64) / np.linalg.norm(ref64))
+    rel32 = max_rel(got, ref64)
+    print(f"\nFP64-ERROR advection 4096^2 x500: max abs fp32 {err32:.3e} (max rel {rel32:.3e}), "
+          f"bf16 storage max abs {errb:.3e}, relative L2 {relb:.3e}")
+    # measured on GB300: fp32 6.9e-6 max abs; bf16 storage 0.107 relative L2
+    # (the bound guards against regressions, the parity check is the bit test)
+    assert err32 < 1e-4 and relb < 0.15
+
+
 CROSS5_OFFSETS = [(0, 0), (-1, 0), (1, 0), (0, -1), (0, 1)]
 CROSS5_WEIGHTS = [0.2, 0.3, 0.1, 0.25, 0.15]
 BOX9_OFFSETS = [(-1, -1), (-1, 0), (-1, 1), (0, -1), (0, 0), (0, 1), (1, -1), (1, 0), (1, 1)]
@@ -221,4 +250,44 @@ def test_advection_register_windowed(cuda, oracle_mod, dtype, T, th):
     a, b, u, v = _advect_inputs(700, 333, 6, dtype)
     got = _advect_gpu(cuda, dtype, a, b, u, v, 17, sch=sched(T, 0, th))
     want = oracle_mod.advect(a, b, u, v, 17, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("offsets,weights", [(S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS), (CROSS5_OFFSETS, CROSS5_WEIGHTS),
+                                             (BOX9_OFFSETS, BOX9_WEIGHTS)])
+@pytest.mark.parametrize("W,H", [(517, 389), (3, 3), (130, 5), (257, 600), (1000, 2)])
+@pytest.mark.parametrize("th", [0, 1, 7])
+def test_streaming_one_step_per_pass(cuda, oracle_mod, dtype, offsets, weights, W, H, th):
+    # one step per pass takes the streaming kernel: warps of 32 vectors of
+    # columns marching th-row chunks (0: the default); ragged widths leave
+    # partial vectors and idle lanes, and the ring of each buffer is kept
+    keep = P._Keep()
+    if dtype == "bf16":
+        weights = [float(S.bf16_to_f32(S.f32_to_bf16(np.array([w], np.float32)))[0]) for w in weights]
+    st = P.make_stencil(P.OP_LINEAR, dtype, offsets, weights, keep=keep)
+    a, b = jac_grids(W, H, W + th, dtype)
+    for iters in (1, 2, 5):
+        got = run2d(cuda, st, a, b, iters, sched=sched(1, 0, th), dtype=dtype)
+        want = oracle_mod.lin2d(a, b, offsets, weights, iters, dtype=dtype)
+        assert np.array_equal(bits(got), bits(want)), iters
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+def test_streaming_wide_ring(cuda, oracle_mod, dtype):
+    # a mask range of 2 with reach-1 offsets: only 2 <= h < H-2, 2 <= w < W-2 is written
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, rng=2, keep=keep)
+    a, b = jac_grids(203, 61, 4, dtype)
+    got = run2d(cuda, st, a, b, 7, sched=sched(1, 0, 5), dtype=dtype)
+    want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, 7, dtype=dtype, rng=2)
+    assert np.array_equal(bits(got), bits(want))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H,th", [(700, 333, 0), (129, 17, 3), (1030, 40, 64)])
+def test_advection_streaming(cuda, oracle_mod, dtype, W, H, th):
+    a, b, u, v = _advect_inputs(W, H, 7, dtype)
+    got = _advect_gpu(cuda, dtype, a, b, u, v, 9, sch=sched(1, 0, th))
+    want = oracle_mod.advect(a, b, u, v, 9, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype=dtype)
     assert np.array_equal(bits(got), bits(want))

@@ -173,27 +173,6 @@ def test_jacobi_c1_full_size_and_fp64_error(cuda, oracle_mod):
 
 
 def test_advection_c3_full_size_and_fp64_error(cuda, oracle_mod):
-    # 4096^2, 500 iterations: fp32 bit-exact against the fp32 oracle; the fp32
-    # and bf16-storage errors against the fp64 oracle are reported.
-    W = H = 4096
-    a, b, u, v = S.advect2d(W, H, seed=1)
-    got = _advect_gpu(cuda, "f32", a, b, u, v, 500)
-    want = oracle_mod.advect(a, b, u, v, 500, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX)
-    assert np.array_equal(bits(got), bits(want))
-    ref64 = oracle_mod.advect(a.astype(np.float64), b.astype(np.float64), u.astype(np.float64),
-                              v.astype(np.float64), 500, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype="f64")
-    ab, bb, ub, vb = (S.f32_to_bf16(x) for x in (a, b, u, v))
-    gb = _advect_gpu(cuda, "bf16", ab, bb, ub, vb, 500)
-    err32 = float(np.max(np.abs(got - ref64)))
-    # the bf16 run also stores its winds in bf16: its error includes that of the rounded inputs
-    errb = float(np.max(np.abs(S.bf16_to_f32(gb) - ref64)))
-    rel32 = max_rel(got, ref64)
-    print(f"\nFP64-ERROR advection 4096^2 x500: max abs fp32 {err32:.3e} (max rel {rel32:.3e}), "
-          f"bf16 storage {errb:.3e}")
-    assert err32 < 1e-4 and errb < 0.1
-
-
-def test_advection_c3_full_size_and_fp64_error(cuda, oracle_mod):
     # 4096^2, 500 iterations: fp32 and bf16 storage bit-exact against the
     # oracle; their errors against the fp64 oracle are reported
     W = H = 4096

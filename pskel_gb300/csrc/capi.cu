@@ -330,9 +330,9 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
     for (int n = 0; n < p.nm; ++n) p.wt[n] = st.mask.weights[n];
   }
   if (T == 1) {
-    // one step per pass: the streaming kernel, a warp per 32 vectors of
-    // columns x HC rows (tile_h, default 16)
-    p.TH = (sched && sched->tile_h > 0) ? static_cast<int>(std::min<int64_t>(sched->tile_h, H)) : 16;
+    // one step per pass: the streaming kernel, a warp per 128 columns x HC
+    // rows (tile_h, default 8)
+    p.TH = (sched && sched->tile_h > 0) ? static_cast<int>(std::min<int64_t>(sched->tile_h, H)) : 8;
     p.tiles_y = static_cast<int>((H + p.TH - 1) / p.TH);
     *used = true;
     for (int64_t k = 0; k < iters; ++k) {

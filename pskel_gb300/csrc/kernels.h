@@ -94,8 +94,8 @@ cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const 
                         cudaStream_t s);
 
 // One step of a reach-1 2D stencil of a known shape (opk 0..2) or advection
-// (opk 3), streaming (no temporal blocking): a warp per 32 16-byte vectors of
-// columns x p.TH rows (p.tiles_y row chunks). Buffers, winds and the row
+// (opk 3), streaming (no temporal blocking): a warp per 128 columns x p.TH
+// rows (p.tiles_y row chunks). Buffers, winds and the row
 // pitch must be 16-byte aligned.
 int64_t stream2d_warps(int W, int H, int HC, int dtype);
 cudaError_t stream2d_step(int opk, int dtype, const Stencil2DParams& p, cudaStream_t s);

@@ -3,8 +3,8 @@
 // schedules of one time step per pass, where a step moves every cell through
 // HBM once and temporal blocking has nothing to reuse.
 //
-// Each warp owns 32 16-byte vectors of columns (128 fp32 / 256 bf16 cells) of
-// a chunk of rows and marches down them, keeping rows h-1, h, h+1 in
+// Each warp owns 128 columns (four cells per lane: 16 bytes of fp32, 8 of
+// bf16) of a chunk of rows and marches down them, keeping rows h-1, h, h+1 in
 // registers and loading row h+2 (and the winds of row h+1) while row h is
 // computed: one row ahead, with four row slots rotated by a four-way unrolled
 // march, so no value moves between registers. West/east neighbours come from
@@ -25,16 +25,21 @@ using fast2d::shape_of;
 
 constexpr int kStreamThreads = 256;
 
+// four cells per lane for either storage type: the same lanes-per-cell as
+// fp32 keeps bf16 warps as many and as light as fp32 ones
+template <class TS>
+using LaneVec = Vec4c<TS>;
+
 template <class TS>
 struct Row {
-  Vec16<TS> v;
+  LaneVec<TS> v;
   float l, r;  // the cells west of the first and east of the last element (edge lanes only)
 };
 
 // OpK: 0..2 linear shapes (fast2d::shape_of), 3 = advection.
 template <class TS, int OpK>
-__global__ void __launch_bounds__(kStreamThreads) stream2d_kernel(const __grid_constant__ Stencil2DParams p) {
-  using Vt = Vec16<TS>;
+__global__ void __launch_bounds__(kStreamThreads, 3) stream2d_kernel(const __grid_constant__ Stencil2DParams p) {
+  using Vt = LaneVec<TS>;
   constexpr int V = Vt::V;
   constexpr bool kAdvect = (OpK == 3);
   constexpr int kShape = OpK < 3 ? OpK : 0;
@@ -85,18 +90,14 @@ __global__ void __launch_bounds__(kStreamThreads) stream2d_kernel(const __grid_c
   auto store_row = [&](int h, const float* res) {
     TS* o = dst + (static_cast<int64_t>(h) * pitch + c);
     if (full_vec) {
-      uint32_t w4[4];
       if constexpr (sizeof(TS) == 4) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) w4[k] = __float_as_uint(res[k]);
+        *reinterpret_cast<float4*>(o) = make_float4(res[0], res[1], res[2], res[3]);
       } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const __nv_bfloat162 b = __floats2bfloat162_rn(res[2 * k], res[2 * k + 1]);
-          w4[k] = *reinterpret_cast<const uint32_t*>(&b);
-        }
+        const __nv_bfloat162 b0 = __floats2bfloat162_rn(res[0], res[1]);
+        const __nv_bfloat162 b1 = __floats2bfloat162_rn(res[2], res[3]);
+        *reinterpret_cast<uint2*>(o) =
+            make_uint2(*reinterpret_cast<const uint32_t*>(&b0), *reinterpret_cast<const uint32_t*>(&b1));
       }
-      *reinterpret_cast<uint4*>(o) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
     } else {
 #pragma unroll
       for (int k = 0; k < V; ++k)
@@ -174,7 +175,8 @@ cudaError_t launch(int opk, const Stencil2DParams& p, int blocks, cudaStream_t s
 }  // namespace
 
 int64_t stream2d_warps(int W, int H, int HC, int dtype) {
-  const int V = dtype == 2 ? 8 : 4;
+  (void)dtype;
+  const int V = 4;
   return static_cast<int64_t>((W + 32 * V - 1) / (32 * V)) * ((H + HC - 1) / HC);
 }
 

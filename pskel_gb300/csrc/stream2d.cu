@@ -6,8 +6,8 @@
 // Each warp owns 128 columns (four cells per lane: 16 bytes of fp32, 8 of
 // bf16) of a chunk of rows and marches down them, keeping rows h-1, h, h+1 in
 // registers and loading row h+2 (and the winds of row h+1) while row h is
-// computed: one row ahead, with four row slots rotated by a four-way unrolled
-// march, so no value moves between registers. West/east neighbours come from
+// computed (bf16: rows h+3 and winds h+2), with the row slots rotated by an
+// unrolled march, so no value moves between registers. West/east neighbours come from
 // the adjacent lanes by shuffles; the warp's edge lanes load theirs with the
 // row. Only cells with ring <= h < H-ring and ring <= w < W-ring are written,
 // so each buffer keeps its own ring, as in Stencil2D::runOpenMP
@@ -44,6 +44,9 @@ __global__ void __launch_bounds__(kStreamThreads, 3) stream2d_kernel(const __gri
   constexpr bool kAdvect = (OpK == 3);
   constexpr int kShape = OpK < 3 ? OpK : 0;
   constexpr int kTerms = shape_of<kShape>().n;
+  // rows loaded ahead of the one computed: bf16 rows carry half the bytes, so
+  // they run one row further ahead to keep as many bytes in flight
+  constexpr int kPD = sizeof(TS) == 2 ? 2 : 1;
   const int lane = threadIdx.x & 31;
   const int64_t gw = static_cast<int64_t>(blockIdx.x) * (kStreamThreads / 32) + (threadIdx.x >> 5);
   const int cols = (p.W + 32 * V - 1) / (32 * V);
@@ -105,9 +108,10 @@ __global__ void __launch_bounds__(kStreamThreads, 3) stream2d_kernel(const __gri
     }
   };
 
+  // one row: load row h+1+kPD (and the winds of row h+kPD), then compute row h
   auto step = [&](int h, Row<TS>& dn, Row<TS>& cur, Row<TS>& up, Row<TS>& nx, Vt& uc, Vt& vc, Vt& un, Vt& vn) {
-    ld_row(h + 2, nx);
-    ld_wind(h + 1, un, vn);
+    ld_row(h + 1 + kPD, nx);
+    ld_wind(h + kPD, un, vn);
     // west / east neighbours of the three rows: adjacent lanes, or the edge loads
     float wd = __shfl_up_sync(0xFFFFFFFFu, dn.v.at(V - 1), 1), ed = __shfl_down_sync(0xFFFFFFFFu, dn.v.at(0), 1);
     float wc = __shfl_up_sync(0xFFFFFFFFu, cur.v.at(V - 1), 1), ec = __shfl_down_sync(0xFFFFFFFFu, cur.v.at(0), 1);
@@ -144,20 +148,38 @@ __global__ void __launch_bounds__(kStreamThreads, 3) stream2d_kernel(const __gri
     if (c_ok) store_row(h, res);
   };
 
-  Row<TS> A, B, C, E;
-  Vt uA, vA, uB, vB;
+  // row slots A..E (winds aligned with them), rotated by unrolling the march
+  // 3 + kPD times: no value moves between registers
+  Row<TS> A, B, C, D, E;
+  Vt uA, vA, uB, vB, uC, vC, uD, vD, uE, vE;
   ld_row(hs - 1, A);
   ld_row(hs, B);
   ld_row(hs + 1, C);
-  ld_wind(hs, uA, vA);
-  for (int h = hs; h < he; h += 4) {
-    step(h, A, B, C, E, uA, vA, uB, vB);
-    if (h + 1 >= he) break;
-    step(h + 1, B, C, E, A, uB, vB, uA, vA);
-    if (h + 2 >= he) break;
-    step(h + 2, C, E, A, B, uA, vA, uB, vB);
-    if (h + 3 >= he) break;
-    step(h + 3, E, A, B, C, uB, vB, uA, vA);
+  ld_wind(hs, uB, vB);
+  if constexpr (kPD == 1) {
+    for (int h = hs; h < he; h += 4) {
+      step(h, A, B, C, D, uB, vB, uC, vC);
+      if (h + 1 >= he) break;
+      step(h + 1, B, C, D, A, uC, vC, uD, vD);
+      if (h + 2 >= he) break;
+      step(h + 2, C, D, A, B, uD, vD, uA, vA);
+      if (h + 3 >= he) break;
+      step(h + 3, D, A, B, C, uA, vA, uB, vB);
+    }
+  } else {
+    ld_row(hs + 2, D);
+    ld_wind(hs + 1, uC, vC);
+    for (int h = hs; h < he; h += 5) {
+      step(h, A, B, C, E, uB, vB, uD, vD);
+      if (h + 1 >= he) break;
+      step(h + 1, B, C, D, A, uC, vC, uE, vE);
+      if (h + 2 >= he) break;
+      step(h + 2, C, D, E, B, uD, vD, uA, vA);
+      if (h + 3 >= he) break;
+      step(h + 3, D, E, A, C, uE, vE, uB, vB);
+      if (h + 4 >= he) break;
+      step(h + 4, E, A, B, D, uA, vA, uC, vC);
+    }
   }
 }
 

@@ -210,6 +210,16 @@ PSKEL_API pskel_status pskel_time2d(const pskel_stencil* st, void* in, void* out
                                     int64_t pitch, int64_t iterations, const pskel_schedule* scheds, int32_t n,
                                     int32_t reps, double* ms, void* stream);
 
+/* The cost of one grid inside a batched launch (pskel_batch_*), for tuning
+ * batches: for each schedule, `copies` copies of a width x height grid with
+ * buffers carved from the caller's device `pool` (cleared to zero first) run
+ * as one batch, `reps` timed runs after an untimed one; ms[i] = median batch
+ * time / copies. The copies give the GPU about two waves of tiles, as many as
+ * the pool holds; copies_used (may be NULL) receives their number. */
+PSKEL_API pskel_status pskel_time_batch2d(const pskel_stencil* st, void* pool, int64_t pool_bytes, int64_t width,
+                                          int64_t height, int64_t iterations, const pskel_schedule* scheds,
+                                          int32_t n, int32_t reps, double* ms, int32_t* copies_used, void* stream);
+
 /* The reference's GA with its analytic objective (solve2D/objective2D,
  * PSkelStencil.hpp:1883-1941: simple GA, two 16-bit genes, population
  * `popsize`, `ngen` generations, pmut 0.01, pcross 0.6), its (tile height,

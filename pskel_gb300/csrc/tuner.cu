@@ -181,6 +181,68 @@ pskel_status pskel_time2d(const pskel_stencil* st, void* in, void* out, int64_t 
   return pskel_sync(stream);
 }
 
+pskel_status pskel_time_batch2d(const pskel_stencil* st, void* pool, int64_t pool_bytes, int64_t width,
+                                int64_t height, int64_t iterations, const pskel_schedule* scheds, int32_t n,
+                                int32_t reps, double* ms, int32_t* copies_used, void* stream) {
+  clear_error();
+  if (!st || !pool || pool_bytes <= 0 || !scheds || !ms || n <= 0 || reps <= 0 || width <= 0 || height <= 0)
+    return fail(PSKEL_ERR_INVALID, "time_batch2d: bad arguments");
+  const int64_t esz = st->dtype == PSKEL_BF16 ? 2 : 4;
+  const int64_t pitch = ((width * esz + 15) / 16) * 16 / esz;
+  const int64_t buf = ((pitch * height * esz + 255) / 256) * 256;
+  const int64_t fit = pool_bytes / (2 * buf);
+  if (fit < 1) return fail(PSKEL_ERR_INVALID, "time_batch2d: the pool holds no copy of the grid");
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(pool, 0, static_cast<size_t>(std::min<int64_t>(pool_bytes, 2 * buf * fit)), s);
+  if (e != cudaSuccess) return cuda_fail(e, "time_batch2d pool clear");
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  std::vector<float> t(reps);
+  pskel_status q = PSKEL_OK;
+  for (int32_t i = 0; i < n && q == PSKEL_OK; ++i) {
+    // enough copies for two waves of tiles of the batched kernel (two CTAs
+    // per SM), as many as the pool holds
+    const TileEstimate g = estimate_tiles(*st, width, height, iterations, scheds[i]);
+    const int64_t tiles = ((width + g.TW - 1) / g.TW) * ((height + g.TH - 1) / g.TH);
+    const int64_t want = std::max<int64_t>(1, (4 * static_cast<int64_t>(sms) + tiles - 1) / tiles);
+    const int64_t copies = std::min<int64_t>(want, fit);
+    std::vector<pskel_batch_grid> grids(static_cast<size_t>(copies));
+    for (int64_t k = 0; k < copies; ++k) {
+      pskel_batch_grid& G = grids[static_cast<size_t>(k)];
+      G.in = static_cast<char*>(pool) + (2 * k) * buf;
+      G.out = static_cast<char*>(pool) + (2 * k + 1) * buf;
+      G.width = width;
+      G.height = height;
+      G.pitch = pitch;
+      G.iterations = iterations;
+      G.schedule = scheds[i];
+    }
+    pskel_batch* bt = nullptr;
+    q = pskel_batch_create(st, grids.data(), static_cast<int32_t>(copies), &bt);
+    if (q != PSKEL_OK) break;
+    q = pskel_batch_run(bt, stream);  // untimed first run
+    for (int32_t r = 0; r < reps && q == PSKEL_OK; ++r) {
+      cudaEventRecord(a, s);
+      q = pskel_batch_run(bt, stream);
+      cudaEventRecord(b, s);
+      cudaEventSynchronize(b);
+      cudaEventElapsedTime(&t[r], a, b);
+    }
+    if (q == PSKEL_OK) q = pskel_sync(stream);
+    pskel_batch_destroy(bt);
+    std::sort(t.begin(), t.end());
+    ms[i] = t[reps / 2] / static_cast<double>(copies);
+    if (copies_used) copies_used[i] = static_cast<int32_t>(copies);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return q;
+}
+
 // The reference's genetic search (solve2D/objective2D, PSkelStencil.hpp:
 // 1883-1941) restated: a simple GA (GAlib 2.4.7's GASimpleGA, absent from the
 // reference tree) over two 16-bit binary-to-decimal genes, tile height h in

@@ -31,6 +31,9 @@ def _setup():
     L.pskel_time2d.argtypes = [C.POINTER(P.Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                C.c_int64, C.POINTER(P.Schedule), C.c_int32, C.c_int32, C.POINTER(C.c_double),
                                C.c_void_p]
+    L.pskel_time_batch2d.argtypes = [C.POINTER(P.Stencil), C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                     C.POINTER(P.Schedule), C.c_int32, C.c_int32, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int32), C.c_void_p]
     L.pskel_ga_schedule2d.argtypes = [C.POINTER(P.Stencil), C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_int32,
                                       C.c_int32, C.POINTER(P.Schedule), C.POINTER(C.c_double)]
     L.pskel_schedule_features2d.argtypes = [C.POINTER(P.Stencil), C.c_int64, C.c_int64, C.c_int64,
@@ -76,6 +79,18 @@ def time_schedules(st: P.Stencil, a, b, iterations: int, scheds, reps: int = 3, 
     P._check(P.lib.pskel_time2d(C.byref(st), P._ptr(a), P._ptr(b), W, H, pitch, iterations, arr, len(scheds), reps,
                                 ms, stream))
     return np.array(ms[:], dtype=np.float64)
+
+
+def time_in_batch(st: P.Stencil, pool, W: int, H: int, iterations: int, scheds, reps: int = 3, stream=None):
+    """Median ms per grid of each schedule inside a batched launch of copies of
+    the grid (buffers from the device tensor `pool`, overwritten)."""
+    arr = (P.Schedule * len(scheds))(*scheds)
+    ms = (C.c_double * len(scheds))()
+    cp = (C.c_int32 * len(scheds))()
+    nbytes = pool.numel() * pool.element_size()
+    P._check(P.lib.pskel_time_batch2d(C.byref(st), P._ptr(pool), nbytes, W, H, iterations, arr, len(scheds), reps,
+                                      ms, cp, stream))
+    return np.array(ms[:], dtype=np.float64), np.array(cp[:], dtype=np.int64)
 
 
 def exhaustive(st: P.Stencil, a, b, iterations: int, reps: int = 3, pitch: int = 0, width=None, height=None):

@@ -441,12 +441,12 @@ def run_batch(args, wl, world, rank, local):
     # ---- tuning (untimed). The measured tuner times each grid's candidates
     # inside a batched launch (copies of the grid filling the GPU, buffers from
     # a scratch pool): the exhaustive per-grid pick on the benchmark's grids.
-    pool = torch.empty(160 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+    scratch = torch.empty(160 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
     t0 = time.perf_counter()
     exh, exh_ms = [], []
     for W, H, it in shapes:
         cs = cands(W, H, it)
-        ms, _ = T.time_in_batch(st, pool, W, H, it, cs, reps=3, stream=sp)
+        ms, _ = T.time_in_batch(st, scratch, W, H, it, cs, reps=3, stream=sp)
         exh.append(cs[int(np.argmin(ms))].time_steps)
         exh_ms.append(float(ms.min()))
     t_exh = time.perf_counter() - t0
@@ -456,11 +456,11 @@ def run_batch(args, wl, world, rank, local):
     X, Y = [], []
     for W, H, it in tshapes:
         cs = cands(W, H, it)
-        ms, _ = T.time_in_batch(st, pool, W, H, it, cs, reps=3, stream=sp)
+        ms, _ = T.time_in_batch(st, scratch, W, H, it, cs, reps=3, stream=sp)
         for c, m in zip(cs, ms):
             X.append(T.features(st, W, H, it, c))
             Y.append(np.log(m))
-    del pool
+    del scratch
     X = np.stack(X)
     Y = np.array(Y, dtype=np.float32)
     model = T.CostModel(hidden=64, layers=3, seed=1)

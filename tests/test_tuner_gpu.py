@@ -173,3 +173,17 @@ def test_trained_model_beats_default_and_ga(cuda):
         assert T.sched_tuple(T.auto_schedule(st, W, H, it)) == T.sched_tuple(m.pick(st, W, H, it))
     finally:
         m.close()
+
+
+def test_time_in_batch(cuda):
+    torch = cuda
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "bf16", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    pool = torch.empty(8 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    cands = [c for c in T.candidates(st, 100, 70, 40) if c.tile_h == 0]
+    ms, copies = T.time_in_batch(st, pool, 100, 70, 40, cands, reps=3)
+    assert np.all(ms > 0) and np.all(copies >= 1)
+    # a small grid is replicated to fill the GPU, as far as the pool allows
+    assert copies.max() > 1
+    with pytest.raises(P.PskelError):
+        T.time_in_batch(st, pool[:1024], 100, 70, 40, cands[:1])

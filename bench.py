@@ -87,8 +87,12 @@ class ClockSampler:
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.file,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.file,
                                          stderr=subprocess.DEVNULL)
+            # the timed region starts once the sampler is producing samples
+            t0 = time.time()
+            while time.time() - t0 < 5 and self.proc.poll() is None and os.path.getsize(self.file.name) == 0:
+                time.sleep(0.02)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self

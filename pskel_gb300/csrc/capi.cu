@@ -589,7 +589,7 @@ static pskel_status stream3d_cross7(const pskel_stencil& st, Stencil3DParams& p,
   CUtensorMap maps[2];
   const uint64_t dims[3] = {static_cast<uint64_t>(D) * esz / 4, static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
   const uint64_t strides[2] = {static_cast<uint64_t>(D) * esz, static_cast<uint64_t>(D) * esz * W};
-  const uint32_t box[3] = {static_cast<uint32_t>(stream3d_tma_box_words(dtype)), 18, 1};
+  const uint32_t box[3] = {136, 18, 1};
   cudaError_t e = encode_tmap(&maps[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, in, dims, strides, box);
   if (e == cudaSuccess) e = encode_tmap(&maps[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, out, dims, strides, box);
   if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled (3D planes)");

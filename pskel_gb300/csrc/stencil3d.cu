@@ -329,30 +329,22 @@ __global__ void __launch_bounds__(256)
 
 // The 7-point cross (centre, h-1, h+1, w-1, w+1, d-1, d+1, summed in that
 // order), one step per launch, with the planes staged in shared memory by TMA.
-// A persistent block owns work items of 128 d cells (four per lane: 16 bytes
-// of fp32, 8 of bf16) x 16 w rows x p.HC planes. A producer warp streams the
-// planes h0-1 .. h1 of its items, one 3D TMA copy per plane of a box of the
-// 128 d cells plus 16 bytes each side (so every copy starts 16-byte aligned)
-// x 18 rows (a row of halo each side), positions outside the grid
-// zero-filled, into a ring of kS3Slots slots. Each slot has a "full" mbarrier
-// (the copy landed) and an "empty" one (all eight consumer warps are done
-// with it), so consumer warps run independently of each other, up to the
-// ring's depth. A consumer reads each plane's rows from shared memory once,
-// widened to fp32, and keeps planes h-1, h, h+1 in registers, rotated by a
-// three-way unrolled march. Every wait is bounded. With a zero halo value the
-// zero fill is the halo; otherwise out-of-grid positions are replaced by it.
+// A persistent block owns work items of 32 vectors of d (128 fp32 / 256 bf16
+// cells) x 16 w rows x p.HC planes. A producer warp streams the planes h0-1 ..
+// h1 of its items, one 3D TMA copy per plane of the 34-vector x 18-row box
+// (a vector and a row of halo on each side; positions outside the grid are
+// zero-filled), into a ring of kS3Slots slots. Each slot has a "full"
+// mbarrier (the copy landed) and an "empty" one (all eight consumer warps
+// have read it), so consumer warps run independently of each other, up to
+// the ring's depth. Every wait is bounded. With a zero halo value the zero
+// fill is the halo; otherwise out-of-grid positions are replaced by it.
 constexpr int kS3Slots = 6;
+constexpr int kS3BoxX = 34;                 // 16-byte vectors per staged row
+constexpr int kS3RowBytes = kS3BoxX * 16;   // 544
 constexpr int kS3BoxY = 18;                 // 16 rows + one each side
+constexpr int kS3PlaneBytes = (kS3RowBytes * kS3BoxY + 127) & ~127;
 constexpr int kS3Consumers = 8;             // consumer warps, two w rows each
 constexpr int kS3Threads = 32 * (kS3Consumers + 1);
-constexpr int kS3Cells = 128;               // d cells per work item
-
-template <class TS>
-struct S3Geom {
-  static constexpr int kRowBytes = 16 + kS3Cells * static_cast<int>(sizeof(TS)) + 16;
-  static constexpr int kPlaneBytes = (kRowBytes * kS3BoxY + 127) & ~127;
-  static constexpr int kBoxWords = kRowBytes / 4;
-};
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -363,17 +355,12 @@ __device__ __forceinline__ void consumers_sync() {
   asm volatile("bar.sync 1, %0;" ::"n"(32 * kS3Consumers) : "memory");
 }
 
-// four cells widened to fp32
-struct F4 {
-  float v[4];
-};
-
 template <class TS, bool kReport, bool kZeroHalo>
 __global__ void __launch_bounds__(kS3Threads, 3)
     stream3d_tma_kernel(const __grid_constant__ CUtensorMap map, const __grid_constant__ Stencil3DParams p) {
   using S = Storage<TS>;
-  using G = S3Geom<TS>;
-  constexpr int ES = static_cast<int>(sizeof(TS));
+  using Vt = Vec16<TS>;
+  constexpr int V = Vt::V;
   extern __shared__ __align__(128) uint8_t smem_raw[];
   __shared__ double s_part[kS3Consumers];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -381,7 +368,7 @@ __global__ void __launch_bounds__(kS3Threads, 3)
     if (tid == 0) atomicOr(p.err, kDevErrAlign);
     return;
   }
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + kS3Slots * G::kPlaneBytes);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + kS3Slots * kS3PlaneBytes);
   uint64_t* empty = full + kS3Slots;
   if (tid == 0) {
     for (int i = 0; i < kS3Slots; ++i) {
@@ -393,12 +380,12 @@ __global__ void __launch_bounds__(kS3Threads, 3)
   __syncthreads();
 
   const int H = p.H, W = p.W, D = p.D;
-  const int dblocks = (D + kS3Cells - 1) / kS3Cells, wblocks = (W + 15) / 16;
+  const int dblocks = (D + 32 * V - 1) / (32 * V), wblocks = (W + 15) / 16;
   const int64_t items = static_cast<int64_t>(dblocks) * wblocks * p.hchunks;
   auto geometry = [&](int64_t it, int& d0, int& w0, int& h0, int& h1) {
     const int db = static_cast<int>(it % dblocks);
     const int64_t r = it / dblocks;
-    d0 = db * kS3Cells;
+    d0 = db * 32 * V;
     w0 = static_cast<int>(r % wblocks) * 16;
     h0 = static_cast<int>(r / wblocks) * p.HC;
     h1 = min(H, h0 + p.HC);
@@ -413,14 +400,13 @@ __global__ void __launch_bounds__(kS3Threads, 3)
       for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
         int d0, w0, h0, h1;
         geometry(it, d0, w0, h0, h1);
-        // the map addresses the grid as 32-bit words; the box starts 16 bytes
-        // before d0 (an x coordinate that is a multiple of four words)
-        const int x = (d0 * ES - 16) / 4;
+        // the map addresses the grid as 32-bit words (a box row of 136 words)
+        const int x = (d0 - V) * static_cast<int>(sizeof(TS)) / 4;
         for (int q = h0 - 1; q <= h1; ++q) {
           if (use > 0 && !mbar_wait_bounded(&empty[slot], (use - 1) & 1u, p.err)) return;
           fence_proxy_async();
-          mbar_arrive_expect_tx(&full[slot], static_cast<uint32_t>(G::kRowBytes * kS3BoxY));
-          tma_load_3d(smem_raw + slot * G::kPlaneBytes, &map, x, w0 - 1, q, &full[slot]);
+          mbar_arrive_expect_tx(&full[slot], static_cast<uint32_t>(kS3RowBytes * kS3BoxY));
+          tma_load_3d(smem_raw + slot * kS3PlaneBytes, &map, x, w0 - 1, q, &full[slot]);
           if (++slot == kS3Slots) {
             slot = 0;
             ++use;
@@ -435,177 +421,170 @@ __global__ void __launch_bounds__(kS3Threads, 3)
   const int64_t plane = static_cast<int64_t>(W) * D;
   TS* __restrict__ dst = static_cast<TS*>(p.dst);
   const float halo = p.halo;
+  uint32_t hraw;
+  if constexpr (sizeof(TS) == 4) {
+    hraw = __float_as_uint(halo);
+  } else {
+    const uint32_t hb = __bfloat16_as_ushort(__float2bfloat16_rn(halo));
+    hraw = hb | (hb << 16);
+  }
   // this thread's staged rows: row 0 of the box is w0-1
   const int r0 = 2 * warp + 1;
   const uint8_t* const sbase = smem_raw;
-  const int o_row0 = r0 * G::kRowBytes + 16 + lane * 4 * ES;
-  const int o_el = r0 * G::kRowBytes + 16 - ES;                 // d0-1
-  const int o_er = r0 * G::kRowBytes + 16 + kS3Cells * ES;      // d0+128
+  const int o_row0 = r0 * kS3RowBytes + (lane + 1) * 16;
+  const int o_el = r0 * kS3RowBytes + (V - 1) * static_cast<int>(sizeof(TS));  // d0-1
+  const int o_er = r0 * kS3RowBytes + 33 * 16;                                  // d0+32V
   SqDiffAcc acc_res;
-  auto ld4 = [&](int slot, int off, F4& v) {
-    const uint8_t* at = sbase + slot * G::kPlaneBytes + off;
-    if constexpr (ES == 4) {
-      const float4 x = *reinterpret_cast<const float4*>(at);
-      v.v[0] = x.x;
-      v.v[1] = x.y;
-      v.v[2] = x.z;
-      v.v[3] = x.w;
-    } else {
-      const uint2 x = *reinterpret_cast<const uint2*>(at);
-      v.v[0] = __uint_as_float(x.x << 16);
-      v.v[1] = __uint_as_float(x.x & 0xFFFF0000u);
-      v.v[2] = __uint_as_float(x.y << 16);
-      v.v[3] = __uint_as_float(x.y & 0xFFFF0000u);
-    }
+  auto ld = [&](int slot, int off, Vt& v) {
+    const uint4 x = *reinterpret_cast<const uint4*>(sbase + slot * kS3PlaneBytes + off);
+    v.r[0] = x.x;
+    v.r[1] = x.y;
+    v.r[2] = x.z;
+    v.r[3] = x.w;
   };
   auto ld1 = [&](int slot, int off) -> float {
-    return S::load(*reinterpret_cast<const TS*>(sbase + slot * G::kPlaneBytes + off));
+    return S::load(*reinterpret_cast<const TS*>(sbase + slot * kS3PlaneBytes + off));
   };
-  auto fill = [&](F4& v) { v.v[0] = v.v[1] = v.v[2] = v.v[3] = halo; };
   auto next = [](int s) { return s + 1 == kS3Slots ? 0 : s + 1; };
-  auto wait_full = [&](int slot, uint32_t ph) -> bool { return mbar_wait_bounded(&full[slot], ph, p.err); };
-  auto release = [&](int slot) {
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[slot]);
-  };
   bool alive = true;
   // slot and phase parity of the next plane in the sequence
   int s_next = 0;
   uint32_t ph_next = 0;
+  auto wait_full = [&](int slot, uint32_t ph) -> bool { return mbar_wait_bounded(&full[slot], ph, p.err); };
 
   for (int64_t it = blockIdx.x; it < items && alive; it += gridDim.x) {
     int d0, w0, h0, h1;
     geometry(it, d0, w0, h0, h1);
-    const int d = d0 + lane * 4;
+    const int d = d0 + lane * V;
     const int w = w0 + warp * 2;
     const bool d_ok = d < D;
     const bool row0 = d_ok && w < W, row1 = d_ok && w + 1 < W;
     // general halo: which staged values lie outside the grid
     const bool wm_in = row0 && w > 0, wp_in = row1 && w + 2 < W;
-    const bool el_in = d0 > 0, er_in = d0 + kS3Cells < D;
-    // the rows of plane q (loaded as the plane below the one computed)
-    auto rows_of = [&](int slot, int q, F4 (&r)[2]) {
-      ld4(slot, o_row0, r[0]);
-      ld4(slot, o_row0 + G::kRowBytes, r[1]);
-      if constexpr (!kZeroHalo) {
-        if (q < 0 || q >= H || !row0) fill(r[0]);
-        if (q < 0 || q >= H || !row1) fill(r[1]);
+    const bool el_in = d0 > 0, er_in = d0 + 32 * V < D;
+    int s_dn = s_next, s_cur = next(s_dn), s_up = next(s_cur);
+    uint32_t ph_dn = ph_next, ph_cur = ph_next ^ (s_cur == 0 ? 1u : 0u), ph_up = ph_cur ^ (s_up == 0 ? 1u : 0u);
+    if (!wait_full(s_dn, ph_dn) || !wait_full(s_cur, ph_cur)) {
+      alive = false;
+      break;
+    }
+    for (int h = h0; h < h1; ++h) {
+      if (!wait_full(s_up, ph_up)) {
+        alive = false;
+        break;
       }
-    };
-    int s_cur = s_next;
-    uint32_t ph_cur = ph_next;
-    // prologue: plane h0-1 (rows only) and plane h0
-    F4 A[2], B[2], C[2];
-    if (!wait_full(s_cur, ph_cur)) {
-      alive = false;
-      break;
-    }
-    rows_of(s_cur, h0 - 1, A);
-    release(s_cur);
-    s_cur = next(s_cur);
-    ph_cur ^= (s_cur == 0) ? 1u : 0u;
-    if (!wait_full(s_cur, ph_cur)) {
-      alive = false;
-      break;
-    }
-    rows_of(s_cur, h0, B);
-
-    // one plane h: rows of h+1 into `up`, sides of h, release h, compute h
-    auto step = [&](int h, F4 (&dn)[2], F4 (&cur)[2], F4 (&up)[2]) -> bool {
-      int s_up = next(s_cur);
-      const uint32_t ph_up = ph_cur ^ ((s_up == 0) ? 1u : 0u);
-      if (!wait_full(s_up, ph_up)) return false;
-      rows_of(s_up, h + 1, up);
-      F4 wm, wp;
-      ld4(s_cur, o_row0 - G::kRowBytes, wm);
-      ld4(s_cur, o_row0 + 2 * G::kRowBytes, wp);
+      Vt dn[2], cur[2], up[2], wm, wp;
+      ld(s_dn, o_row0, dn[0]);
+      ld(s_dn, o_row0 + kS3RowBytes, dn[1]);
+      ld(s_cur, o_row0, cur[0]);
+      ld(s_cur, o_row0 + kS3RowBytes, cur[1]);
+      ld(s_up, o_row0, up[0]);
+      ld(s_up, o_row0 + kS3RowBytes, up[1]);
+      ld(s_cur, o_row0 - kS3RowBytes, wm);
+      ld(s_cur, o_row0 + 2 * kS3RowBytes, wp);
       float el[2] = {0.0f, 0.0f}, er[2] = {0.0f, 0.0f};
       if (lane == 0) {
         el[0] = ld1(s_cur, o_el);
-        el[1] = ld1(s_cur, o_el + G::kRowBytes);
+        el[1] = ld1(s_cur, o_el + kS3RowBytes);
       }
       if (lane == 31) {
         er[0] = ld1(s_cur, o_er);
-        er[1] = ld1(s_cur, o_er + G::kRowBytes);
+        er[1] = ld1(s_cur, o_er + kS3RowBytes);
       }
-      release(s_cur);  // plane h is read for the last time
-      s_cur = s_up;
-      ph_cur = ph_up;
+      // plane h-1 is read for the last time
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s_dn]);
       if constexpr (!kZeroHalo) {
-        if (!wm_in) fill(wm);
-        if (!wp_in) fill(wp);
+        if (h - 1 < 0) {
+          dn[0].fill(hraw);
+          dn[1].fill(hraw);
+        }
+        if (h + 1 >= H) {
+          up[0].fill(hraw);
+          up[1].fill(hraw);
+        }
+        if (!row0) {
+          dn[0].fill(hraw);
+          cur[0].fill(hraw);
+          up[0].fill(hraw);
+        }
+        if (!row1) {
+          dn[1].fill(hraw);
+          cur[1].fill(hraw);
+          up[1].fill(hraw);
+        }
+        if (!wm_in) wm.fill(hraw);
+        if (!wp_in) wp.fill(hraw);
         if (!el_in) el[0] = el[1] = halo;
         if (!er_in) er[0] = er[1] = halo;
       }
       TS* out = dst + (h * plane + static_cast<int64_t>(w) * D + d);
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
-        float dl = __shfl_up_sync(0xFFFFFFFFu, cur[j].v[3], 1);
-        float dr = __shfl_down_sync(0xFFFFFFFFu, cur[j].v[0], 1);
+        float dl = __shfl_up_sync(0xFFFFFFFFu, cur[j].at(V - 1), 1);
+        float dr = __shfl_down_sync(0xFFFFFFFFu, cur[j].at(0), 1);
         if (lane == 0) dl = el[j];
         if (lane == 31) dr = er[j];
-        const F4& a = (j == 0) ? wm : cur[0];
-        const F4& b = (j == 0) ? cur[1] : wp;
+        const Vt& a = (j == 0) ? wm : cur[0];
+        const Vt& b = (j == 0) ? cur[1] : wp;
         const bool row_ok = (j == 0) ? row0 : row1;
-        float res[4];
+        uint32_t o[4];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const float l = (c == 0) ? dl : cur[j].v[c - 1];
-          const float r = (c == 3) ? dr : cur[j].v[c + 1];
-          float acc = __fmul_rn(p.wt[0], cur[j].v[c]);
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[1], dn[j].v[c]));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[2], up[j].v[c]));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[3], a.v[c]));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[4], b.v[c]));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[5], l));
-          acc = __fadd_rn(acc, __fmul_rn(p.wt[6], r));
-          res[c] = acc;
-        }
-        float stored[4];
-        if constexpr (ES == 4) {
+        for (int g = 0; g < V / 4; ++g) {
+          float res[4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) stored[c] = res[c];
-          if (row_ok) *reinterpret_cast<float4*>(out + j * D) = make_float4(res[0], res[1], res[2], res[3]);
-        } else {
-          const __nv_bfloat162 b0 = __floats2bfloat162_rn(res[0], res[1]);
-          const __nv_bfloat162 b1 = __floats2bfloat162_rn(res[2], res[3]);
-          const uint32_t u0 = *reinterpret_cast<const uint32_t*>(&b0);
-          const uint32_t u1 = *reinterpret_cast<const uint32_t*>(&b1);
-          stored[0] = __uint_as_float(u0 << 16);
-          stored[1] = __uint_as_float(u0 & 0xFFFF0000u);
-          stored[2] = __uint_as_float(u1 << 16);
-          stored[3] = __uint_as_float(u1 & 0xFFFF0000u);
-          if (row_ok) *reinterpret_cast<uint2*>(out + j * D) = make_uint2(u0, u1);
-        }
-        if (kReport && row_ok) {
+          for (int k = 0; k < 4; ++k) {
+            const int c = 4 * g + k;
+            const float l = (c == 0) ? dl : cur[j].at(c - 1);
+            const float r = (c == V - 1) ? dr : cur[j].at(c + 1);
+            float acc = __fmul_rn(p.wt[0], cur[j].at(c));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[1], dn[j].at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[2], up[j].at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[3], a.at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[4], b.at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[5], l));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[6], r));
+            res[k] = acc;
+          }
+          float stored[4];
+          if constexpr (sizeof(TS) == 4) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) acc_res.add(stored[c], cur[j].v[c]);
+            for (int k = 0; k < 4; ++k) {
+              o[k] = __float_as_uint(res[k]);
+              stored[k] = res[k];
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              const __nv_bfloat162 bb = __floats2bfloat162_rn(res[2 * k], res[2 * k + 1]);
+              o[2 * g + k] = *reinterpret_cast<const uint32_t*>(&bb);
+              stored[2 * k] = __uint_as_float(o[2 * g + k] << 16);
+              stored[2 * k + 1] = __uint_as_float(o[2 * g + k] & 0xFFFF0000u);
+            }
+          }
+          if (kReport && row_ok) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc_res.add(stored[k], cur[j].at(4 * g + k));
+          }
         }
+        if (row_ok) *reinterpret_cast<uint4*>(out + j * D) = make_uint4(o[0], o[1], o[2], o[3]);
       }
-      return true;
-    };
-
-    for (int h = h0; h < h1 && alive; h += 3) {
-      if (!step(h, A, B, C)) {
-        alive = false;
-        break;
-      }
-      if (h + 1 >= h1) break;
-      if (!step(h + 1, B, C, A)) {
-        alive = false;
-        break;
-      }
-      if (h + 2 >= h1) break;
-      if (!step(h + 2, C, A, B)) {
-        alive = false;
-        break;
-      }
+      s_dn = s_cur;
+      ph_dn = ph_cur;
+      s_cur = s_up;
+      ph_cur = ph_up;
+      s_up = next(s_up);
+      ph_up ^= (s_up == 0) ? 1u : 0u;
     }
     if (!alive) break;
-    // plane h1 was read only as the plane above the last one computed
-    release(s_cur);
-    s_next = next(s_cur);
-    ph_next = ph_cur ^ ((s_next == 0) ? 1u : 0u);
+    // planes h1-1 and h1 are released at the end of the item
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(&empty[s_dn]);
+      mbar_arrive(&empty[s_cur]);
+    }
+    s_next = s_up;
+    ph_next = ph_up;
   }
   if constexpr (kReport) {
     double v = acc_res.value();
@@ -682,22 +661,11 @@ int64_t stream3d_ctas(int W, int D, int hchunks) {
   return static_cast<int64_t>((D + 31) / 32) * ((W + 7) / 8) * hchunks;
 }
 
-template <class TS>
-size_t tma_smem_bytes() {
-  return kS3Slots * S3Geom<TS>::kPlaneBytes + 16 * kS3Slots;
-}
-
-size_t stream3d_tma_smem_bytes(int dtype) {
-  return dtype == 2 ? tma_smem_bytes<__nv_bfloat16>() : tma_smem_bytes<float>();
-}
-
-int stream3d_tma_box_words(int dtype) {
-  return dtype == 2 ? S3Geom<__nv_bfloat16>::kBoxWords : S3Geom<float>::kBoxWords;
-}
+size_t stream3d_tma_smem_bytes() { return kS3Slots * kS3PlaneBytes + 16 * kS3Slots; }
 
 template <class TS>
 int tma_blocks_per_sm() {
-  const size_t smem = tma_smem_bytes<TS>();
+  const size_t smem = stream3d_tma_smem_bytes();
   void* ks[4] = {reinterpret_cast<void*>(stream3d_tma_kernel<TS, false, false>),
                  reinterpret_cast<void*>(stream3d_tma_kernel<TS, false, true>),
                  reinterpret_cast<void*>(stream3d_tma_kernel<TS, true, false>),
@@ -717,13 +685,13 @@ int stream3d_tma_blocks_per_sm(int dtype) {
 }
 
 int64_t stream3d_tma_items(int W, int D, int hchunks, int esize) {
-  (void)esize;
-  return static_cast<int64_t>((D + kS3Cells - 1) / kS3Cells) * ((W + 15) / 16) * hchunks;
+  const int kD = 32 * (16 / esize);
+  return static_cast<int64_t>((D + kD - 1) / kD) * ((W + 15) / 16) * hchunks;
 }
 
 template <class TS>
 void launch_tma(const CUtensorMap* map, const Stencil3DParams& p, int ctas, bool report, cudaStream_t s) {
-  const size_t smem = tma_smem_bytes<TS>();
+  const size_t smem = stream3d_tma_smem_bytes();
   uint32_t hbits;
   std::memcpy(&hbits, &p.halo, sizeof(hbits));
   const bool zero = hbits == 0u;  // +0.0 exactly: the TMA zero fill is the halo

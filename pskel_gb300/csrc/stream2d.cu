@@ -38,7 +38,7 @@ struct Row {
 
 // OpK: 0..2 linear shapes (fast2d::shape_of), 3 = advection.
 template <class TS, int OpK>
-__global__ void __launch_bounds__(kStreamThreads, 4) stream2d_kernel(const __grid_constant__ Stencil2DParams p) {
+__global__ void __launch_bounds__(kStreamThreads, sizeof(TS) == 2 ? 4 : 3) stream2d_kernel(const __grid_constant__ Stencil2DParams p) {
   using Vt = LaneVec<TS>;
   constexpr int V = Vt::V;
   constexpr bool kAdvect = (OpK == 3);

@@ -208,75 +208,80 @@ static bool tma_ok(const void* p, int64_t pitch_bytes) {
 
 // ------------------------------------------------------------- 2D iterate
 
+// Game of Life on bit planes: both grids are packed once into two global bit
+// planes (L2-resident for grids up to ~16k x 16k), the passes run between the
+// planes, and the final plane's interior is unpacked into the result buffer.
+// The other buffer is not written; ring cells of the result keep their bytes.
 static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
                                  int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,
                                  cudaStream_t s) {
-  LifeGeom g;
-  const int per_sm = life_max_ctas_per_sm(256);
+  (void)st;
+  if (iters <= 0) return PSKEL_OK;
+  const int per_sm = life_bits_ctas_per_sm();
+  const int64_t slots = static_cast<int64_t>(per_sm) * c->sms;
   const int64_t it1 = std::max<int64_t>(iters, 1);
-  auto geom_for = [&](int T, LifeGeom& out) -> bool {
-    T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeMaxT), it1));
+  struct Geo {
+    int T, TH;
+  };
+  auto geom_for = [&](int T, Geo& g) -> bool {
+    T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeBitsMaxT), it1));
     if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
     int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
-    TH = std::min(TH, 256 - 2 * T) & ~1;
-    if (TH < 2) return false;
-    out.T = T;
-    out.TH = TH;
-    out.LH = TH + 2 * T;
-    out.tiles_x = static_cast<int>((W + kLifeTW - 1) / kLifeTW);
-    out.tiles_y = static_cast<int>((H + TH - 1) / TH);
-    const int ntiles = out.tiles_x * out.tiles_y;
-    out.ctas = (sched && sched->ctas > 0) ? sched->ctas : per_sm * c->sms;
-    out.ctas = std::max(1, std::min(out.ctas, ntiles));
+    TH = std::min(TH, 256 - 2 * T);
+    if (TH < 1) return false;
+    g.T = T;
+    g.TH = TH;
     return true;
   };
+  Geo g{1, 254};
   if (sched && sched->time_steps > 0) {
     if (!geom_for(sched->time_steps, g))
       return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", sched->time_steps);
   } else {
-    // Default schedule: every tile costs about the same (the bit planes are
-    // always 256 rows), so the run costs (passes) x (waves of tiles over the
-    // resident CTAs). Pick the odd temporal block minimising that product.
+    // Default: a tile always computes 256 rows, so a pass costs about
+    // waves x (T + 2) (two step-equivalents of staging); minimise passes x that.
     double best = 0;
     bool found = false;
-    for (int T = kLifeMaxT - 1; T >= 5; T -= 2) {
-      LifeGeom cand;
+    for (int T = kLifeBitsMaxT; T >= 5; T -= 2) {
+      Geo cand;
       if (!geom_for(T, cand)) continue;
       const int64_t passes = static_cast<int64_t>(plan_passes(iters, cand.T).size());
-      const int64_t slots = static_cast<int64_t>(per_sm) * c->sms;
-      const int64_t waves = (static_cast<int64_t>(cand.tiles_x) * cand.tiles_y + slots - 1) / slots;
-      const double cost = static_cast<double>(passes) * static_cast<double>(waves);
+      const int64_t waves = (life_bits_tiles(static_cast<int>(W), static_cast<int>(H), cand.TH) + slots - 1) / slots;
+      const double cost = static_cast<double>(passes) * static_cast<double>(waves) * (cand.T + 2);
       if (!found || cost < best) {
         best = cost;
         g = cand;
         found = true;
       }
-      if (cand.T < T) break;  // iterations cap the block: smaller T only adds passes
+      if (cand.T < T) break;  // iterations cap the block
     }
     if (!found && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
   }
-  const bool use_tma = tma_ok(in, pitch) && tma_ok(out, pitch);
-  CUtensorMap map_in, map_out;
-  memset(&map_in, 0, sizeof(map_in));
-  memset(&map_out, 0, sizeof(map_out));
-  if (use_tma) {
-    const uint64_t dims[2] = {static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
-    const uint64_t strides[1] = {static_cast<uint64_t>(pitch)};
-    const uint32_t box[2] = {static_cast<uint32_t>(kLifeLW), 64u};  // one 64-row chunk per load
-    cudaError_t e = encode_tmap(&map_in, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, in, dims, strides, box);
-    if (e == cudaSuccess) e = encode_tmap(&map_out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, out, dims, strides, box);
-    if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled");
-  }
+  const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), g.TH);
+  int ctas = (sched && sched->ctas > 0) ? sched->ctas : static_cast<int>(slots);
+  ctas = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(ctas, tiles)));
+  const size_t plane = static_cast<size_t>(life_bits_words(static_cast<int>(W))) * static_cast<size_t>(H);
+  if (pskel_status q = ensure_buffer(c->life_bits, 2 * plane * sizeof(uint32_t))) return q;
+  uint32_t* A = static_cast<uint32_t*>(c->life_bits.ptr);
+  uint32_t* B = A + plane;
+  cudaError_t e = life_bits_pack(static_cast<const uint8_t*>(in), pitch, static_cast<int>(W), static_cast<int>(H), A,
+                                 ring, false, c->err, c->sms, s);
+  if (e == cudaSuccess)
+    e = life_bits_pack(static_cast<const uint8_t*>(out), pitch, static_cast<int>(W), static_cast<int>(H), B, ring,
+                       true, c->err, c->sms, s);
+  if (e != cudaSuccess) return cuda_fail(e, "Life pack launch");
   const std::vector<int> passes = plan_passes(iters, g.T);
   for (size_t i = 0; i < passes.size(); ++i) {
     const bool fwd = (i % 2 == 0);
-    const uint8_t* src = static_cast<const uint8_t*>(fwd ? in : out);
-    uint8_t* dst = static_cast<uint8_t*>(fwd ? out : in);
-    cudaError_t e = life_pass(fwd ? &map_in : &map_out, fwd ? &map_out : &map_in, use_tma, src, dst, static_cast<int>(W), static_cast<int>(H),
-                              pitch, ring, passes[i], g, c->err, s);
+    e = life_bits_pass(fwd ? A : B, fwd ? B : A, static_cast<int>(W), static_cast<int>(H), ring, passes[i], g.T, g.TH,
+                       ctas, s);
     if (e != cudaSuccess) return cuda_fail(e, "Life kernel launch");
   }
-  (void)st;
+  // an odd number of passes (odd iterations) ends in B, whose result goes to `out`
+  const bool odd = (passes.size() % 2) == 1;
+  e = life_bits_unpack(odd ? B : A, static_cast<uint8_t*>(odd ? out : in), pitch, static_cast<int>(W),
+                       static_cast<int>(H), ring, c->sms, s);
+  if (e != cudaSuccess) return cuda_fail(e, "Life unpack launch");
   return PSKEL_OK;
 }
 

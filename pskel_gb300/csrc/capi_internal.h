@@ -23,6 +23,7 @@ struct DeviceContext {
   DeviceBuffer host_in, host_out, host_u, host_v;  // staging for *_host
   DeviceBuffer partials;                           // 3D residual: per-CTA fp64 partial sums
   DeviceBuffer residuals;                          // 3D residual norms for *_host
+  DeviceBuffer life_bits;                          // Life: the two bit planes of a run
 };
 
 pskel_status fail(pskel_status code, const char* fmt, ...);

@@ -41,6 +41,22 @@ cudaError_t life_pass(const CUtensorMap* map_src, const CUtensorMap* map_dst, bo
                       int64_t pitch, int ring, int steps, const LifeGeom& g, unsigned* err, cudaStream_t s);
 int life_max_ctas_per_sm(int LH);
 
+// Bit-plane Life: pack both grids once into global bit planes (rows of
+// life_bits_words(W) words), run the passes between the planes, unpack the
+// final plane's interior into the result buffer. Tiles: 16 words x (TH + 2T)
+// rows with one word and T rows of halo, T <= kLifeBitsMaxT.
+constexpr int kLifeBitsMaxT = 31;
+int life_bits_words(int W);
+size_t life_bits_smem_bytes();
+int life_bits_ctas_per_sm();
+int life_bits_tiles(int W, int H, int TH);
+cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
+                           unsigned* err, int sms, cudaStream_t s);
+cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring, int sms,
+                             cudaStream_t s);
+cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
+                           int ctas, cudaStream_t s);
+
 // ------------------------------------------------------- 2D float stencils
 
 enum class Op2D { Linear, Advect };

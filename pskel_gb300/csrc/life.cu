@@ -80,15 +80,17 @@ constexpr uint32_t kSelect = 0xCA;    // a ? b : c, bitwise
 // the twos. With k0 folded in, count in {2, 3} <=> ~y1 & (x1 ^ k0), and the
 // cell lives iff that holds and (s0 | alive): count 3, or count 2 and alive.
 // A count of 8 leaves y1 set, so it is dead as it must be.
-template <bool kMasked>
+// P: the bit plane's row pitch in words (a zero row above row 0 and a zero
+// word left of word 0, so word (row, j) sits at (row + 1) * P + j + 1).
+template <bool kMasked, int P = kBitPitch>
 __device__ __forceinline__ void life_strip(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int y0, int j,
                                            uint32_t colmask, int gy0, int ring, int H) {
   uint32_t c[kRowsPerStrip + 2], t0[kRowsPerStrip + 2], t1[kRowsPerStrip + 2];
   uint32_t p0[kRowsPerStrip + 2], p1[kRowsPerStrip + 2];
-  const uint32_t* base = in + bit_index(y0 - 1, j);
+  const uint32_t* base = in + (y0 * P + j + 1);  // row y0 - 1
 #pragma unroll
   for (int k = 0; k < kRowsPerStrip + 2; ++k) {
-    const uint32_t* r = base + k * kBitPitch;
+    const uint32_t* r = base + k * P;
     const uint32_t l = r[-1], cc = r[0], e = r[1];
     const uint32_t we = __funnelshift_l(l, cc, 1);  // bit b = cell b-1
     const uint32_t ea = __funnelshift_r(cc, e, 1);  // bit b = cell b+1
@@ -98,7 +100,7 @@ __device__ __forceinline__ void life_strip(const uint32_t* __restrict__ in, uint
     p0[k] = we ^ ea;
     p1[k] = we & ea;
   }
-  uint32_t* o = out + bit_index(y0, j);
+  uint32_t* o = out + ((y0 + 1) * P + j + 1);
 #pragma unroll
   for (int k = 1; k <= kRowsPerStrip; ++k) {
     const uint32_t s0 = lop3<kXor3>(t0[k - 1], p0[k], t0[k + 1]);
@@ -107,7 +109,7 @@ __device__ __forceinline__ void life_strip(const uint32_t* __restrict__ in, uint
     const uint32_t y1 = lop3<kMaj>(t1[k - 1], p1[k], t1[k + 1]);
     const uint32_t two_or_three = lop3<kNotAAndBxC>(y1, x1, k0);
     const uint32_t alive = lop3<kAAndBorC>(two_or_three, s0, c[k]);
-    uint32_t* dst = o + (k - 1) * kBitPitch;
+    uint32_t* dst = o + (k - 1) * P;
     if (kMasked) {
       // cells outside r <= h < H-r, r <= w < W-r keep the value this plane holds
       const int gy = gy0 + y0 + k - 1;
@@ -321,7 +323,202 @@ __global__ void __launch_bounds__(kLifeThreads, 3)
   if (bad_value) atomicOr(err, kDevErrValue);
 }
 
+// ---------------------------------------------------------------------------
+// Bit-plane passes. A run packs the source and destination grids once into
+// two global bit planes (one bit per cell, rows of PW words), runs every pass
+// between the planes -- 16 MB for an 8192^2 grid, resident in L2 -- and
+// unpacks the final plane into the result buffer's interior once. A pass
+// tile is 16 words (512 cells) x LH rows with one word (32 cells) and T rows
+// of halo on each side, staged by cp.async into a shared bit plane.
+constexpr int kBW = 16;                          // words per loaded tile row
+constexpr int kBCore = kBW - 2;                  // core words
+constexpr int kBP = kBW + 2;                     // shared plane pitch (zero word each side)
+constexpr int kBRows = 256;
+constexpr int kBPlane = (kBRows + 2) * kBP;      // words per shared plane
+constexpr int kBThreads = kBW * (kBRows / kRowsPerStrip);  // 512: a word column x an 8-row strip each
+
+// packs rows of `src` (bytes 0/1) into a bit plane; check: 0 = every cell must
+// be 0/1, 1 = only the ring (the interior of a destination is overwritten
+// before it is read)
+__global__ void __launch_bounds__(256) life_pack_kernel(const uint8_t* __restrict__ src, int64_t pitch, int W, int H,
+                                                        uint32_t* __restrict__ plane, int PW, int ring, int check,
+                                                        unsigned* err) {
+  bool bad = false;
+  const int64_t n = static_cast<int64_t>(H) * PW;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int row = static_cast<int>(i / PW), wd = static_cast<int>(i - static_cast<int64_t>(row) * PW);
+    const int c0 = wd * 32;
+    const uint8_t* r = src + static_cast<int64_t>(row) * pitch;
+    const bool row_ring = row < ring || row >= H - ring;
+    uint32_t bits = 0;
+    if (c0 + 32 <= W && (reinterpret_cast<uintptr_t>(r + c0) & 15) == 0) {
+      const uint4 a = *reinterpret_cast<const uint4*>(r + c0);
+      const uint4 b = *reinterpret_cast<const uint4*>(r + c0 + 16);
+      const uint32_t any = a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w;
+      if (any & 0xFEFEFEFEu) {
+        for (int k = 0; k < 32; ++k) {
+          const uint8_t v = r[c0 + k];
+          const bool in_ring = row_ring || c0 + k < ring || c0 + k >= W - ring;
+          if (v > 1 && (check == 0 || in_ring)) bad = true;
+        }
+      }
+      const uint4 am = make_uint4(a.x & 0x01010101u, a.y & 0x01010101u, a.z & 0x01010101u, a.w & 0x01010101u);
+      const uint4 bm = make_uint4(b.x & 0x01010101u, b.y & 0x01010101u, b.z & 0x01010101u, b.w & 0x01010101u);
+      bits = pack16(am) | (pack16(bm) << 16);
+    } else {
+      for (int k = 0; k < 32 && c0 + k < W; ++k) {
+        const uint8_t v = r[c0 + k];
+        const bool in_ring = row_ring || c0 + k < ring || c0 + k >= W - ring;
+        if (v > 1 && (check == 0 || in_ring)) bad = true;
+        bits |= static_cast<uint32_t>(v & 1u) << k;
+      }
+    }
+    plane[i] = bits;
+  }
+  if (bad) atomicOr(err, kDevErrValue);
+}
+
+// writes the interior cells (ring <= h < H-ring, ring <= w < W-ring) of a bit
+// plane into `dst` as bytes; ring cells of `dst` are left as they are
+__global__ void __launch_bounds__(256) life_unpack_kernel(const uint32_t* __restrict__ plane, int PW, uint8_t* dst,
+                                                          int64_t pitch, int W, int H, int ring) {
+  const int rows = H - 2 * ring;
+  if (rows <= 0) return;
+  const int64_t n = static_cast<int64_t>(rows) * PW;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int row = ring + static_cast<int>(i / PW), wd = static_cast<int>(i % PW);
+    const int c0 = wd * 32;
+    if (c0 >= W - ring || c0 + 32 <= ring) continue;
+    const uint32_t bits = plane[static_cast<int64_t>(row) * PW + wd];
+    uint8_t* r = dst + static_cast<int64_t>(row) * pitch;
+    if (c0 >= ring && c0 + 32 <= W - ring && (reinterpret_cast<uintptr_t>(r + c0) & 15) == 0) {
+      *reinterpret_cast<uint4*>(r + c0) = unpack16(bits & 0xFFFFu);
+      *reinterpret_cast<uint4*>(r + c0 + 16) = unpack16(bits >> 16);
+    } else {
+      for (int k = 0; k < 32; ++k) {
+        const int c = c0 + k;
+        if (c >= ring && c < W - ring) r[c] = static_cast<uint8_t>((bits >> k) & 1u);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src, bool valid) {
+  const int n = valid ? 4 : 0;  // zero-fill when the source word lies outside the plane
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One pass of `steps` (<= T) generations from plane `src` to plane `dst`.
+__global__ void __launch_bounds__(kBThreads, 2)
+    life_bits_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int PW, int W, int H, int ring,
+                     int steps, int T, int TH, int LH, int tiles_x, int tiles_y) {
+  extern __shared__ __align__(128) uint32_t bsm[];
+  uint32_t* planeA = bsm;
+  uint32_t* planeB = bsm + kBPlane;
+  const int tid = threadIdx.x;
+  // the zero borders (row -1, row LH.., word -1, word 16) are never written
+  for (int i = tid; i < 2 * kBPlane; i += kBThreads) bsm[i] = 0u;
+  __syncthreads();
+  const int j = tid & (kBW - 1);
+  const int y0 = (tid / kBW) * kRowsPerStrip;
+  const int ntiles = tiles_x * tiles_y;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    const int gy0 = ty * TH - T;
+    const int gw0 = tx * kBCore - 1;
+    const int gx0 = gw0 * 32;
+    const bool ring_tile = (gy0 < ring) || (gy0 + LH > H - ring) || (gx0 < ring) || (gx0 + kBW * 32 > W - ring);
+    // ring tiles also stage the destination's tile: its ring bits are read by
+    // the odd steps and written back unchanged with the core words
+    const int nstage = ring_tile ? 2 : 1;
+    // stage the source tile (and, for ring tiles, the destination's) by cp.async
+    for (int k = 0; k < nstage; ++k) {
+      const uint32_t* g = (k == 0) ? src : dst;
+      uint32_t* pl = (k == 0) ? planeA : planeB;
+      for (int i = tid; i < LH * kBW; i += kBThreads) {
+        const int row = i / kBW, wd = i - row * kBW;
+        const int gy = gy0 + row, gw = gw0 + wd;
+        const bool ok = gy >= 0 && gy < H && gw >= 0 && gw < PW;
+        cp_async4(pl + (row + 1) * kBP + wd + 1, ok ? g + static_cast<int64_t>(gy) * PW + gw : g, ok);
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // rows at or beyond LH stay zero from the last tile only if LH is the
+    // same; clear them (they feed only the halo, but keep them defined)
+    for (int i = LH * kBW + tid; i < kBRows * kBW; i += kBThreads) {
+      const int row = i / kBW, wd = i - row * kBW;
+      planeA[(row + 1) * kBP + wd + 1] = 0u;
+      planeB[(row + 1) * kBP + wd + 1] = 0u;
+    }
+    __syncthreads();
+    const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
+    for (int s = 0; s < steps; ++s) {
+      const uint32_t* in = (s & 1) ? planeB : planeA;
+      uint32_t* out = (s & 1) ? planeA : planeB;
+      if (ring_tile) {
+        life_strip<true, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+      } else {
+        life_strip<false, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+      }
+      __syncthreads();
+    }
+    // core words -> destination plane
+    const uint32_t* fin = (steps & 1) ? planeB : planeA;
+    for (int i = tid; i < TH * kBCore; i += kBThreads) {
+      const int r = i / kBCore, wd = 1 + (i - r * kBCore);
+      const int row = T + r;
+      const int gy = gy0 + row, gw = gw0 + wd;
+      if (gy < 0 || gy >= H || gw >= PW) continue;
+      dst[static_cast<int64_t>(gy) * PW + gw] = fin[(row + 1) * kBP + wd + 1];
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
+
+int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
+
+int life_bits_tiles(int W, int H, int TH) {
+  return ((life_bits_words(W) + kBCore - 1) / kBCore) * ((H + TH - 1) / TH);
+}
+
+size_t life_bits_smem_bytes() { return 2 * static_cast<size_t>(kBPlane) * sizeof(uint32_t); }
+
+int life_bits_ctas_per_sm() {
+  int n = 0;
+  const size_t smem = life_bits_smem_bytes();
+  cudaFuncSetAttribute(life_bits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_kernel, kBThreads, smem) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
+                           unsigned* err, int sms, cudaStream_t s) {
+  const int PW = life_bits_words(W);
+  life_pack_kernel<<<4 * sms, 256, 0, s>>>(src, pitch, W, H, plane, PW, ring, ring_only ? 1 : 0, err);
+  return cudaGetLastError();
+}
+
+cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring, int sms,
+                             cudaStream_t s) {
+  life_unpack_kernel<<<4 * sms, 256, 0, s>>>(plane, life_bits_words(W), dst, pitch, W, H, ring);
+  return cudaGetLastError();
+}
+
+cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
+                           int ctas, cudaStream_t s) {
+  const int LH = TH + 2 * T;
+  const int tiles_x = (life_bits_words(W) + kBCore - 1) / kBCore;
+  const int tiles_y = (H + TH - 1) / TH;
+  life_bits_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(src, dst, life_bits_words(W), W, H, ring, steps,
+                                                                     T, TH, LH, tiles_x, tiles_y);
+  return cudaGetLastError();
+}
 
 size_t life_smem_bytes(int LH) {
   (void)LH;

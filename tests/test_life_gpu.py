@@ -31,7 +31,7 @@ def test_life_matches_oracle(cuda, oracle_mod, W, H, iters):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("T", [1, 2, 3, 8, 13, 16])
+@pytest.mark.parametrize("T", [1, 2, 3, 8, 13, 16, 21, 31])
 @pytest.mark.parametrize("tile_h", [0, 2, 40])
 def test_life_schedules(cuda, oracle_mod, T, tile_h):
     keep = P._Keep()
@@ -53,7 +53,7 @@ def test_life_mask_order_and_range(cuda, oracle_mod):
 
 @pytest.mark.parametrize("pitch", [517, 520, 1024])
 def test_life_pitched_and_unaligned(cuda, oracle_mod, pitch):
-    # pitch 517 is not a multiple of 16 bytes: the kernel stages tiles without TMA
+    # pitch 517 is not a multiple of 16 bytes: rows are packed with byte loads
     keep = P._Keep()
     a, b = grids(513, 301, seed=pitch)
     got = run2d(cuda, life_stencil(keep), a, b, 21, pitch=pitch, dtype="u8")
@@ -111,3 +111,13 @@ def test_life_full_size_vs_oracle_and_schedule_invariance(cuda, oracle_mod):
                dtype="u8")
     assert np.array_equal(r16, r7)
     assert 0 < int(r16.sum()) < r16.size
+
+
+@pytest.mark.parametrize("ctas", [1, 3])
+def test_life_few_ctas_many_tiles(cuda, oracle_mod, ctas):
+    # persistent CTAs walk many tiles each, ring tiles and interior ones
+    keep = P._Keep()
+    a, b = grids(1100, 600, seed=ctas)
+    got = run2d(cuda, life_stencil(keep), a, b, 23,
+                sched=dict(time_steps=9, tile_w=0, tile_h=50, tile_d=0, ctas=ctas), dtype="u8")
+    assert np.array_equal(got, oracle_mod.life(a, b, 23))

@@ -238,22 +238,27 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
     if (!geom_for(sched->time_steps, g))
       return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", sched->time_steps);
   } else {
-    // Default: a tile always computes 256 rows, so a pass costs about
-    // waves x (T + 2) (two step-equivalents of staging); minimise passes x that.
+    // Default: a tile computes its loaded rows (TH + 2T, in 16-row warp
+    // strips) for T steps plus about two steps' worth of staging, and the
+    // tiles of a pass run in waves over the resident CTAs. Minimise
+    // passes x waves x strips x (T + 2) over T and TH.
     double best = 0;
     bool found = false;
-    for (int T = kLifeBitsMaxT; T >= 5; T -= 2) {
-      Geo cand;
-      if (!geom_for(T, cand)) continue;
-      const int64_t passes = static_cast<int64_t>(plan_passes(iters, cand.T).size());
-      const int64_t waves = (life_bits_tiles(static_cast<int>(W), static_cast<int>(H), cand.TH) + slots - 1) / slots;
-      const double cost = static_cast<double>(passes) * static_cast<double>(waves) * (cand.T + 2);
-      if (!found || cost < best) {
-        best = cost;
-        g = cand;
-        found = true;
+    for (int T = kLifeBitsMaxT; T >= 1; T -= 2) {
+      Geo base;
+      if (!geom_for(T, base)) continue;
+      const int64_t passes = static_cast<int64_t>(plan_passes(iters, base.T).size());
+      for (int TH = base.TH; TH >= std::max(8, base.TH / 4); --TH) {
+        const int64_t waves = (life_bits_tiles(static_cast<int>(W), static_cast<int>(H), TH) + slots - 1) / slots;
+        const int strips = (TH + 2 * base.T + 15) / 16;
+        const double cost = static_cast<double>(passes) * static_cast<double>(waves) * strips * (base.T + 2);
+        if (!found || cost < best) {
+          best = cost;
+          g = Geo{base.T, TH};
+          found = true;
+        }
       }
-      if (cand.T < T) break;  // iterations cap the block
+      if (base.T < T) break;  // iterations cap the block
     }
     if (!found && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
   }

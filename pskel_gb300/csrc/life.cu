@@ -456,13 +456,18 @@ __global__ void __launch_bounds__(kBThreads, 2)
     }
     __syncthreads();
     const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
+    // strips wholly below the loaded rows stay zero and are skipped: a tile
+    // costs its loaded height, not the plane's 256 rows
+    const bool active = y0 < LH;
     for (int s = 0; s < steps; ++s) {
       const uint32_t* in = (s & 1) ? planeB : planeA;
       uint32_t* out = (s & 1) ? planeA : planeB;
-      if (ring_tile) {
-        life_strip<true, kBP>(in, out, y0, j, colmask, gy0, ring, H);
-      } else {
-        life_strip<false, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+      if (active) {
+        if (ring_tile) {
+          life_strip<true, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+        } else {
+          life_strip<false, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+        }
       }
       __syncthreads();
     }

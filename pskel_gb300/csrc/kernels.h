@@ -21,26 +21,6 @@ std::vector<int> plan_passes(int64_t iters, int T);
 
 // ------------------------------------------------------------------ Life
 
-struct LifeGeom {
-  int T;      // max steps per pass (halo rows), <= 16
-  int TH;     // core rows per tile
-  int LH;     // loaded rows per tile = TH + 2T (<= 256, even)
-  int tiles_x, tiles_y;
-  int ctas;
-};
-
-constexpr int kLifeLW = 256;                 // loaded bytes per tile row (TMA box width)
-constexpr int kLifeHX = 16;                  // horizontal halo, bytes
-constexpr int kLifeTW = kLifeLW - 2 * kLifeHX;  // 224 core columns
-constexpr int kLifeMaxT = 16;
-constexpr int kLifeThreads = 256;
-
-size_t life_smem_bytes(int LH);
-// One pass of `steps` (<= geom.T) Life steps from src to dst.
-cudaError_t life_pass(const CUtensorMap* map_src, const CUtensorMap* map_dst, bool use_tma, const uint8_t* src, uint8_t* dst, int W, int H,
-                      int64_t pitch, int ring, int steps, const LifeGeom& g, unsigned* err, cudaStream_t s);
-int life_max_ctas_per_sm(int LH);
-
 // Bit-plane Life: pack both grids once into global bit planes (rows of
 // life_bits_words(W) words), run the passes between the planes, unpack the
 // final plane's interior into the result buffer. Tiles: 16 words x (TH + 2T)

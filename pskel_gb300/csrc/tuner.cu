@@ -70,11 +70,11 @@ TileEstimate estimate_tiles(const pskel_stencil& st, int64_t W, int64_t H, int64
     return std::max(T, 1);
   };
   if (st.op == PSKEL_OP_LIFE) {
-    g.T = clamp_odd(s.time_steps > 0 ? s.time_steps : 15, kLifeMaxT);
+    g.T = clamp_odd(s.time_steps > 0 ? s.time_steps : 15, kLifeBitsMaxT);
     g.TH = std::max(2, (s.tile_h > 0 ? std::min(s.tile_h, 256 - 2 * g.T) : 256 - 2 * g.T) & ~1);
     g.LH = g.TH + 2 * g.T;
-    g.TW = kLifeTW;
-    g.LW = kLifeLW;
+    g.TW = 448;  // 14 core words of the 16-word bit-plane tile
+    g.LW = 512;
     g.tall = false;
   } else if (fast_path(st)) {
     const int vec = st.dtype == PSKEL_BF16 ? 8 : 4;
@@ -130,7 +130,7 @@ int32_t pskel_candidates2d(const pskel_stencil* st, int64_t width, int64_t heigh
   std::vector<pskel_schedule> c;
   const int64_t it = std::max<int64_t>(iterations, 1);
   if (st->op == PSKEL_OP_LIFE) {
-    for (int T = 1; T <= kLifeMaxT && T <= it; T += 2) c.push_back(sched(0, 0, T));
+    for (int T = 1; T <= kLifeBitsMaxT && T <= it; T += 2) c.push_back(sched(0, 0, T));
   } else if (fast_path(*st)) {
     for (int T = 1; T <= 15 && T <= it; T += 2)
       for (int th : {0, 130}) c.push_back(sched(0, th, T));

@@ -212,42 +212,38 @@ static bool tma_ok(const void* p, int64_t pitch_bytes) {
 // planes (L2-resident for grids up to ~16k x 16k), the passes run between the
 // planes, and the final plane's interior is unpacked into the result buffer.
 // The other buffer is not written; ring cells of the result keep their bytes.
-// Game of Life on bit planes: both grids are packed once into two global bit
-// planes (L2-resident for grids up to ~16k x 16k), the passes run between the
-// planes, and the final plane's interior is unpacked into the result buffer.
-// The other buffer is not written; ring cells of the result keep their bytes.
 static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
                                  int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,
                                  cudaStream_t s) {
   (void)st;
   if (iters <= 0) return PSKEL_OK;
+  const int per_sm = life_bits_ctas_per_sm();
+  const int64_t slots = static_cast<int64_t>(per_sm) * c->sms;
   const int64_t it1 = std::max<int64_t>(iters, 1);
-  int T = (sched && sched->time_steps > 0) ? sched->time_steps : 15;  // 15: fastest per generation measured
-  T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeBitsMaxT), it1));
-  if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
-  int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
-  TH = std::min(TH, 256 - 2 * T);
-  if (TH < 1) return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", T);
-  // tile width: the one that runs a pass in the fewest rounds of tiles over
-  // the resident CTAs, weighted by its width (a tile's cost)
-  // (schedule.tile_w, when set, names the loaded width in cells: 512, 576, 640 or 768)
-  int bw = 16;
-  bool found = false;
-  double best = 0;
-  for (int cand : {16, 18, 20, 24}) {
-    if (sched && sched->tile_w > 0 && cand * 32 != sched->tile_w) continue;
-    const int64_t cslots = static_cast<int64_t>(life_bits_ctas_per_sm(cand)) * c->sms;
-    const int64_t ctiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), TH, cand);
-    const double cost = static_cast<double>((ctiles + cslots - 1) / cslots) * cand;
-    if (!found || cost < best) {
-      best = cost;
-      bw = cand;
-      found = true;
-    }
+  struct Geo {
+    int T, TH;
+  };
+  auto geom_for = [&](int T, Geo& g) -> bool {
+    T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeBitsMaxT), it1));
+    if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
+    int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
+    TH = std::min(TH, 256 - 2 * T);
+    if (TH < 1) return false;
+    g.T = T;
+    g.TH = TH;
+    return true;
+  };
+  Geo g{1, 254};
+  if (sched && sched->time_steps > 0) {
+    if (!geom_for(sched->time_steps, g))
+      return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", sched->time_steps);
+  } else {
+    // Default: 15 generations per pass on full-height tiles (256 loaded rows)
+    // -- the fastest per generation on GB300 among 7..31 (measured: 13 and 21
+    // are 3-6 % slower, shorter tiles lose more to their fixed costs).
+    if (!geom_for(15, g) && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
   }
-  if (!found) return fail(PSKEL_ERR_INVALID, "Life tile width %d: not one of 512, 576, 640, 768", sched->tile_w);
-  const int64_t slots = static_cast<int64_t>(life_bits_ctas_per_sm(bw)) * c->sms;
-  const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), TH, bw);
+  const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), g.TH);
   int ctas = (sched && sched->ctas > 0) ? sched->ctas : static_cast<int>(slots);
   ctas = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(ctas, tiles)));
   const size_t plane = static_cast<size_t>(life_bits_words(static_cast<int>(W))) * static_cast<size_t>(H);
@@ -260,10 +256,10 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
     e = life_bits_pack(static_cast<const uint8_t*>(out), pitch, static_cast<int>(W), static_cast<int>(H), B, ring,
                        true, c->err, c->sms, s);
   if (e != cudaSuccess) return cuda_fail(e, "Life pack launch");
-  const std::vector<int> passes = plan_passes(iters, T);
+  const std::vector<int> passes = plan_passes(iters, g.T);
   for (size_t i = 0; i < passes.size(); ++i) {
     const bool fwd = (i % 2 == 0);
-    e = life_bits_pass(fwd ? A : B, fwd ? B : A, static_cast<int>(W), static_cast<int>(H), ring, passes[i], T, TH, bw,
+    e = life_bits_pass(fwd ? A : B, fwd ? B : A, static_cast<int>(W), static_cast<int>(H), ring, passes[i], g.T, g.TH,
                        ctas, s);
     if (e != cudaSuccess) return cuda_fail(e, "Life kernel launch");
   }

@@ -23,21 +23,19 @@ std::vector<int> plan_passes(int64_t iters, int T);
 
 // Bit-plane Life: pack both grids once into global bit planes (rows of
 // life_bits_words(W) words), run the passes between the planes, unpack the
-// final plane's interior into the result buffer. Tiles: bw words (16, 18, 20
-// or 24) x (TH + 2T) rows with one word and T rows of halo, T <= kLifeBitsMaxT;
-// bw x 32 threads per CTA.
+// final plane's interior into the result buffer. Tiles: 16 words x (TH + 2T)
+// rows with one word and T rows of halo, T <= kLifeBitsMaxT.
 constexpr int kLifeBitsMaxT = 31;
 int life_bits_words(int W);
-size_t life_bits_smem_bytes(int bw);
-int life_bits_threads(int bw);
-int life_bits_ctas_per_sm(int bw);
-int life_bits_tiles(int W, int H, int TH, int bw);
+size_t life_bits_smem_bytes();
+int life_bits_ctas_per_sm();
+int life_bits_tiles(int W, int H, int TH);
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
                            unsigned* err, int sms, cudaStream_t s);
 cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring, int sms,
                              cudaStream_t s);
 cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
-                           int bw, int ctas, cudaStream_t s);
+                           int ctas, cudaStream_t s);
 
 // ------------------------------------------------------- 2D float stencils
 

@@ -123,18 +123,12 @@ __device__ __forceinline__ void life_strip(const uint32_t* __restrict__ in, uint
 // unpacks the final plane into the result buffer's interior once. A pass
 // tile is 16 words (512 cells) x LH rows with one word (32 cells) and T rows
 // of halo on each side, staged by cp.async into a shared bit plane.
-// Tile geometry for a loaded width of BW words: BW - 2 core words, a shared
-// plane pitch with a zero word each side, chosen so that the two 8-row strips
-// a warp can span land on different banks (pitch = 2 mod 4), and one thread
-// per word column and 8-row strip.
+constexpr int kBW = 16;                          // words per loaded tile row
+constexpr int kBCore = kBW - 2;                  // core words
+constexpr int kBP = kBW + 2;                     // shared plane pitch (zero word each side)
 constexpr int kBRows = 256;
-template <int BW>
-struct BitTile {
-  static constexpr int kCore = BW - 2;
-  static constexpr int kPitch = ((BW + 2) % 4 == 2) ? BW + 2 : BW + 4;
-  static constexpr int kPlane = (kBRows + 2) * kPitch;
-  static constexpr int kThreads = BW * (kBRows / kRowsPerStrip);
-};
+constexpr int kBPlane = (kBRows + 2) * kBP;      // words per shared plane
+constexpr int kBThreads = kBW * (kBRows / kRowsPerStrip);  // 512: a word column x an 8-row strip each
 
 // packs rows of `src` (bytes 0/1) into a bit plane; check: 0 = every cell must
 // be 0/1, 1 = only the ring (the interior of a destination is overwritten
@@ -211,12 +205,9 @@ __device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src, bo
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // One pass of `steps` (<= T) generations from plane `src` to plane `dst`.
-template <int BW>
-__global__ void __launch_bounds__(BitTile<BW>::kThreads, 2)
+__global__ void __launch_bounds__(kBThreads, 2)
     life_bits_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int PW, int W, int H, int ring,
                      int steps, int T, int TH, int LH, int tiles_x, int tiles_y) {
-  using TG = BitTile<BW>;
-  constexpr int kBW = BW, kBCore = TG::kCore, kBP = TG::kPitch, kBPlane = TG::kPlane, kBThreads = TG::kThreads;
   extern __shared__ __align__(128) uint32_t bsm[];
   uint32_t* planeA = bsm;
   uint32_t* planeB = bsm + kBPlane;
@@ -224,7 +215,7 @@ __global__ void __launch_bounds__(BitTile<BW>::kThreads, 2)
   // the zero borders (row -1, row LH.., word -1, word 16) are never written
   for (int i = tid; i < 2 * kBPlane; i += kBThreads) bsm[i] = 0u;
   __syncthreads();
-  const int j = tid % kBW;
+  const int j = tid & (kBW - 1);
   const int y0 = (tid / kBW) * kRowsPerStrip;
   const int ntiles = tiles_x * tiles_y;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -290,38 +281,17 @@ __global__ void __launch_bounds__(BitTile<BW>::kThreads, 2)
 
 int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
 
-int life_bits_tiles(int W, int H, int TH, int bw) {
-  return ((life_bits_words(W) + (bw - 2) - 1) / (bw - 2)) * ((H + TH - 1) / TH);
+int life_bits_tiles(int W, int H, int TH) {
+  return ((life_bits_words(W) + kBCore - 1) / kBCore) * ((H + TH - 1) / TH);
 }
 
-namespace {
-template <int BW>
-void* bits_kernel_ptr() {
-  return reinterpret_cast<void*>(life_bits_kernel<BW>);
-}
-void* bits_kernel(int bw) {
-  switch (bw) {
-    case 18: return bits_kernel_ptr<18>();
-    case 20: return bits_kernel_ptr<20>();
-    case 24: return bits_kernel_ptr<24>();
-    default: return bits_kernel_ptr<16>();
-  }
-}
-}  // namespace
+size_t life_bits_smem_bytes() { return 2 * static_cast<size_t>(kBPlane) * sizeof(uint32_t); }
 
-size_t life_bits_smem_bytes(int bw) {
-  const int pitch = ((bw + 2) % 4 == 2) ? bw + 2 : bw + 4;
-  return 2 * static_cast<size_t>((kBRows + 2) * pitch) * sizeof(uint32_t);
-}
-
-int life_bits_threads(int bw) { return bw * (kBRows / kRowsPerStrip); }
-
-int life_bits_ctas_per_sm(int bw) {
+int life_bits_ctas_per_sm() {
   int n = 0;
-  const size_t smem = life_bits_smem_bytes(bw);
-  void* k = bits_kernel(bw);
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, life_bits_threads(bw), smem) != cudaSuccess) return 1;
+  const size_t smem = life_bits_smem_bytes();
+  cudaFuncSetAttribute(life_bits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_kernel, kBThreads, smem) != cudaSuccess) return 1;
   return n > 0 ? n : 1;
 }
 
@@ -339,27 +309,12 @@ cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch,
 }
 
 cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
-                           int bw, int ctas, cudaStream_t s) {
+                           int ctas, cudaStream_t s) {
   const int LH = TH + 2 * T;
-  const int PW = life_bits_words(W);
-  const int tiles_x = (PW + (bw - 2) - 1) / (bw - 2);
+  const int tiles_x = (life_bits_words(W) + kBCore - 1) / kBCore;
   const int tiles_y = (H + TH - 1) / TH;
-  const size_t smem = life_bits_smem_bytes(bw);
-  const int threads = life_bits_threads(bw);
-  switch (bw) {
-    case 18:
-      life_bits_kernel<18><<<ctas, threads, smem, s>>>(src, dst, PW, W, H, ring, steps, T, TH, LH, tiles_x, tiles_y);
-      break;
-    case 20:
-      life_bits_kernel<20><<<ctas, threads, smem, s>>>(src, dst, PW, W, H, ring, steps, T, TH, LH, tiles_x, tiles_y);
-      break;
-    case 24:
-      life_bits_kernel<24><<<ctas, threads, smem, s>>>(src, dst, PW, W, H, ring, steps, T, TH, LH, tiles_x, tiles_y);
-      break;
-    default:
-      life_bits_kernel<16><<<ctas, threads, smem, s>>>(src, dst, PW, W, H, ring, steps, T, TH, LH, tiles_x, tiles_y);
-      break;
-  }
+  life_bits_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(src, dst, life_bits_words(W), W, H, ring, steps,
+                                                                     T, TH, LH, tiles_x, tiles_y);
   return cudaGetLastError();
 }
 

@@ -73,8 +73,8 @@ TileEstimate estimate_tiles(const pskel_stencil& st, int64_t W, int64_t H, int64
     g.T = clamp_odd(s.time_steps > 0 ? s.time_steps : 15, kLifeBitsMaxT);
     g.TH = std::max(2, (s.tile_h > 0 ? std::min(s.tile_h, 256 - 2 * g.T) : 256 - 2 * g.T) & ~1);
     g.LH = g.TH + 2 * g.T;
-    g.LW = s.tile_w > 0 ? s.tile_w : 576;  // the bit-plane tile's loaded width (cells)
-    g.TW = g.LW - 64;
+    g.TW = 448;  // 14 core words of the 16-word bit-plane tile
+    g.LW = 512;
     g.tall = false;
   } else if (fast_path(st)) {
     const int vec = st.dtype == PSKEL_BF16 ? 8 : 4;

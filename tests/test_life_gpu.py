@@ -121,15 +121,3 @@ def test_life_few_ctas_many_tiles(cuda, oracle_mod, ctas):
     got = run2d(cuda, life_stencil(keep), a, b, 23,
                 sched=dict(time_steps=9, tile_w=0, tile_h=50, tile_d=0, ctas=ctas), dtype="u8")
     assert np.array_equal(got, oracle_mod.life(a, b, 23))
-
-
-@pytest.mark.parametrize("tile_w", [512, 576, 640, 768])
-@pytest.mark.parametrize("T", [1, 15])
-def test_life_tile_widths(cuda, oracle_mod, tile_w, T):
-    # every bit-plane tile width (16, 18, 20, 24 words loaded) on a grid whose
-    # width is not a multiple of any of them
-    keep = P._Keep()
-    a, b = grids(1501, 333, seed=tile_w + T)
-    got = run2d(cuda, life_stencil(keep), a, b, 31,
-                sched=dict(time_steps=T, tile_w=tile_w, tile_h=0, tile_d=0, ctas=0), dtype="u8")
-    assert np.array_equal(got, oracle_mod.life(a, b, 31))

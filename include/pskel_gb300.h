@@ -127,8 +127,10 @@ PSKEL_API int32_t pskel_plan_passes(int64_t iterations, int32_t time_steps, int3
  * PSkelStencil.hpp:943-1097) and runIterativeTilingGPU's inner temporal
  * blocking (PSkelStencil.h:292, PSkelStencil.hpp:1663-1862): schedule.time_steps
  * plays pyramidHeight / innerIterations, schedule.tile_* the tiling sizes.
- * `pitch` is the row pitch in elements (0 = width). Both buffers are written
- * (ping-pong); see the header comment for where the result ends. */
+ * `pitch` is the row pitch in elements (0 = width). The result ends in `out`
+ * (odd iterations) or `in` (even), with its ring untouched; the other
+ * buffer's contents afterwards are unspecified (the float paths ping-pong
+ * through it, Life runs on internal bit planes and does not write it). */
 PSKEL_API pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height,
                              int64_t pitch, int64_t iterations, const pskel_schedule* sched, void* stream);
 

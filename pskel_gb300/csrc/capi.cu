@@ -321,17 +321,42 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
     for (int n = 0; n < p.nm; ++n) p.wt[n] = st.mask.weights[n];
   }
   if (T == 1) {
-    // one step per pass: the streaming kernel, a warp per 128 columns x HC
-    // rows (tile_h, default 8)
-    p.TH = (sched && sched->tile_h > 0) ? static_cast<int>(std::min<int64_t>(sched->tile_h, H)) : 8;
-    p.tiles_y = static_cast<int>((H + p.TH - 1) / p.TH);
+    // one step per pass: the streaming kernel with rows staged by TMA,
+    // persistent blocks over items of 32 vectors of columns x HC rows
+    // (tile_h; default: about four items per resident block, 8-row groups)
+    const int esz = dtype == PSKEL_BF16 ? 2 : 4;
+    const int64_t resident = static_cast<int64_t>(stream2d_tma_blocks_per_sm(opk, dtype)) * c->sms;
+    const int64_t strips = stream2d_tma_items(static_cast<int>(W), static_cast<int>(H), static_cast<int>(H), dtype);
+    int HC = static_cast<int>((H * strips + 4 * resident - 1) / (4 * resident));
+    HC = std::max(8, ((HC + 7) / 8) * 8);
+    if (sched && sched->tile_h > 0) HC = static_cast<int>(std::min<int64_t>(sched->tile_h, H));
+    p.TH = HC;
+    p.tiles_y = static_cast<int>((H + HC - 1) / HC);
+    const int64_t items = stream2d_tma_items(static_cast<int>(W), static_cast<int>(H), HC, dtype);
+    int ctas = static_cast<int>(std::min<int64_t>(items, resident));
+    if (sched && sched->ctas > 0) ctas = std::min(ctas, sched->ctas);
+    ctas = std::max(ctas, 1);
+    const uint64_t dims[2] = {static_cast<uint64_t>((W * esz + 3) / 4), static_cast<uint64_t>(H)};
+    const uint64_t strides[1] = {static_cast<uint64_t>(pb)};
+    const uint32_t box_phi[2] = {136u, 8u};
+    const uint32_t box_w[2] = {128u, 8u};
+    CUtensorMap m_in, m_out, m_u, m_v;
+    memset(&m_u, 0, sizeof(m_u));
+    memset(&m_v, 0, sizeof(m_v));
+    cudaError_t e = encode_tmap(&m_in, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, in, dims, strides, box_phi);
+    if (e == cudaSuccess) e = encode_tmap(&m_out, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, out, dims, strides, box_phi);
+    if (advect && e == cudaSuccess)
+      e = encode_tmap(&m_u, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(st.wind_u), dims, strides, box_w);
+    if (advect && e == cudaSuccess)
+      e = encode_tmap(&m_v, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(st.wind_v), dims, strides, box_w);
+    if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled (2D rows)");
     *used = true;
     for (int64_t k = 0; k < iters; ++k) {
       const bool fwd = (k % 2 == 0);
       p.src = fwd ? in : out;
       p.dst = fwd ? out : in;
       p.steps = 1;
-      cudaError_t e = stream2d_step(opk, dtype, p, s);
+      e = stream2d_tma_step(opk, dtype, fwd ? &m_in : &m_out, &m_u, &m_v, p, ctas, s);
       if (e != cudaSuccess) return cuda_fail(e, "2D streaming kernel launch");
     }
     return PSKEL_OK;

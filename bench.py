@@ -47,7 +47,7 @@ WORKLOADS = {
     "advect": dict(desc="advection-diffusion 2D, float32 4096x4096, winds N(0,0.1), K 0.1, dt 0.2, 500 iterations",
                    W=4096, H=4096, iters=500, dtype="f32", T=5, b_alg=16),
     "advect_bf16": dict(desc="advection-diffusion 2D, bf16 storage / fp32 arithmetic, 4096x4096, 500 iterations",
-                        W=4096, H=4096, iters=500, dtype="bf16", T=7, b_alg=8),
+                        W=4096, H=4096, iters=500, dtype="bf16", T=1, b_alg=8),
     "heat3d": dict(desc="3D 7-point heat (Mask3D), float32 512^3, zero halo, 50 iterations, fp64 residual every 10",
                    W=512, H=512, D=512, iters=50, dtype="f32", T=1, b_alg=8, every=10),
     "heat3d_bf16": dict(desc="3D 7-point heat, bf16 storage / fp32 arithmetic, 512^3, 50 iterations, "

@@ -328,7 +328,7 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
     const int64_t resident = static_cast<int64_t>(stream2d_tma_blocks_per_sm(opk, dtype)) * c->sms;
     const int64_t strips = stream2d_tma_items(static_cast<int>(W), static_cast<int>(H), static_cast<int>(H), dtype);
     int HC = static_cast<int>((H * strips + 4 * resident - 1) / (4 * resident));
-    HC = std::max(8, ((HC + 7) / 8) * 8);
+    HC = std::max(32, ((HC + 7) / 8) * 8);
     if (sched && sched->tile_h > 0) HC = static_cast<int>(std::min<int64_t>(sched->tile_h, H));
     p.TH = HC;
     p.tiles_y = static_cast<int>((H + HC - 1) / HC);

@@ -143,36 +143,4 @@ struct Vec16 {
   __device__ __forceinline__ void fill(uint32_t h) { r[0] = r[1] = r[2] = r[3] = h; }
 };
 
-// 4 cells kept packed: 16 bytes of fp32 or 8 bytes of bf16, widened on use.
-template <class TS>
-struct Vec4c {
-  static constexpr int V = 4;
-  static constexpr int kWords = sizeof(TS);  // 32-bit words: 4 (fp32) or 2 (bf16)
-  uint32_t r[kWords];
-  __device__ __forceinline__ float at(int c) const {
-    if constexpr (sizeof(TS) == 4) {
-      return __uint_as_float(r[c]);
-    } else {
-      return (c & 1) ? __uint_as_float(r[c >> 1] & 0xFFFF0000u) : __uint_as_float(r[c >> 1] << 16);
-    }
-  }
-  __device__ __forceinline__ void load(const TS* p) {
-    if constexpr (sizeof(TS) == 4) {
-      const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-      r[0] = v.x;
-      r[1] = v.y;
-      r[2] = v.z;
-      r[3] = v.w;
-    } else {
-      const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
-      r[0] = v.x;
-      r[1] = v.y;
-    }
-  }
-  __device__ __forceinline__ void fill(uint32_t h) {
-#pragma unroll
-    for (int i = 0; i < kWords; ++i) r[i] = h;
-  }
-};
-
 }  // namespace pskel

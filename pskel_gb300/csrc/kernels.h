@@ -90,19 +90,15 @@ cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const 
                         cudaStream_t s);
 
 // One step of a reach-1 2D stencil of a known shape (opk 0..2) or advection
-// (opk 3), streaming (no temporal blocking): a warp per 128 columns x p.TH
-// rows (p.tiles_y row chunks). Buffers, winds and the row
-// pitch must be 16-byte aligned.
-int64_t stream2d_warps(int W, int H, int HC, int dtype);
-// The same with rows staged by TMA: persistent blocks (a producer warp and 8
-// consumer warps) over items of 32 16-byte vectors of columns x p.TH rows;
-// `phi` maps the source as 32-bit words with a box of 136 words x 8 rows,
-// `u`/`v` (advection) the winds with a box of 128 words x 8 rows.
+// (opk 3), streaming (no temporal blocking), rows staged by TMA: persistent
+// blocks (a producer warp and 8 consumer warps) over items of 32 16-byte
+// vectors of columns x p.TH rows; `phi` maps the source as 32-bit words with
+// a box of 136 words x 8 rows, `u`/`v` (advection) the winds with a box of
+// 128 words x 8 rows. Buffers, winds and the row pitch 16-byte aligned.
 int stream2d_tma_blocks_per_sm(int opk, int dtype);
 int64_t stream2d_tma_items(int W, int H, int HC, int dtype);
 cudaError_t stream2d_tma_step(int opk, int dtype, const CUtensorMap* phi, const CUtensorMap* u, const CUtensorMap* v,
                               const Stencil2DParams& p, int ctas, cudaStream_t s);
-cudaError_t stream2d_step(int opk, int dtype, const Stencil2DParams& p, cudaStream_t s);
 
 // ------------------------------------------------------- 3D float stencils
 

@@ -277,7 +277,7 @@ pskel_status pskel_batch_create(const pskel_stencil* st, const pskel_batch_grid*
     const int64_t pb = pitch * esz;
     if ((reinterpret_cast<uintptr_t>(G.in) & 15) || (reinterpret_cast<uintptr_t>(G.out) & 15) || (pb & 15))
       return fail(PSKEL_ERR_UNSUPPORTED, "batch grid %d: buffers and row pitch must be 16-byte aligned", i);
-    int T = G.schedule.time_steps > 0 ? G.schedule.time_steps : (dtype == PSKEL_BF16 ? 7 : 3);
+    int T = G.schedule.time_steps > 0 ? G.schedule.time_steps : 7;  // the linear shapes' default
     T = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(G.iterations, 1)));
     if (T > 1 && (T & 1) == 0) --T;
     int HX = 0;

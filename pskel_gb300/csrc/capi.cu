@@ -286,7 +286,7 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
   const int LW = 128;
   const int S = (sched && sched->tile_h > 64) ? 8 : 4;
   const int LH = 16 * S + 2;
-  int T = (sched && sched->time_steps > 0) ? sched->time_steps : (dtype == PSKEL_BF16 ? 7 : 3);
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : fast2d_default_steps(advect, dtype, W, H);
   T = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(iters, 1)));
   if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
   int HX = 0, HY = 0;

@@ -81,6 +81,15 @@ cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* 
 // advection. Shapes (entries in summation order): 0 = N,S,W,E;
 // 1 = C,N,S,W,E; 2 = the 3x3 box row by row. Returns -1 for other masks.
 int fast2d_shape(const int* offsets, int n);
+// The default steps per pass of the reach-1 kernels (measured on GB300):
+// linear shapes 7 (4096^2 fp32: T=5/7 1.32/1.30 T cell updates/s, T=1 0.70);
+// advection fp32 5; advection bf16 1 (the HBM-bound streaming kernel) on
+// grids of 4M cells or more, else 7.
+inline int fast2d_default_steps(bool advect, int dtype, int64_t W, int64_t H) {
+  if (!advect) return 7;
+  if (dtype != 2) return 5;
+  return W * H >= (int64_t(1) << 22) ? 1 : 7;
+}
 size_t fast2d_smem_bytes(bool advect, int dtype, int S);
 int fast2d_max_ctas_per_sm(bool advect, int dtype, int S);
 // opk: a shape above, or 3 for advection. Tile: 128 cells wide, 16 * S + 2

@@ -81,7 +81,8 @@ TileEstimate estimate_tiles(const pskel_stencil& st, int64_t W, int64_t H, int64
     const int S = s.tile_h > 64 ? 8 : 4;
     g.LW = 128;
     g.LH = 16 * S + 2;
-    int T = clamp_odd(s.time_steps > 0 ? s.time_steps : (st.dtype == PSKEL_BF16 ? 7 : 3), 1 << 20);
+    int T = clamp_odd(
+        s.time_steps > 0 ? s.time_steps : fast2d_default_steps(st.op == PSKEL_OP_ADVECT, st.dtype, W, H), 1 << 20);
     int HX = 0;
     for (;;) {
       HX = ((T + vec - 1) / vec) * vec;

@@ -217,8 +217,6 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
                                  cudaStream_t s) {
   (void)st;
   if (iters <= 0) return PSKEL_OK;
-  const int per_sm = life_bits_ctas_per_sm();
-  const int64_t slots = static_cast<int64_t>(per_sm) * c->sms;
   const int64_t it1 = std::max<int64_t>(iters, 1);
   struct Geo {
     int T, TH;
@@ -244,8 +242,10 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
     if (!geom_for(15, g) && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
   }
   const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), g.TH);
-  int ctas = (sched && sched->ctas > 0) ? sched->ctas : static_cast<int>(slots);
-  ctas = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(ctas, tiles)));
+  // every pass in one persistent launch: no more CTAs than can be resident
+  const int64_t resident = static_cast<int64_t>(life_bits_persistent_ctas_per_sm()) * c->sms;
+  int ctas = (sched && sched->ctas > 0) ? sched->ctas : static_cast<int>(resident);
+  ctas = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(ctas, resident), tiles)));
   const size_t plane = static_cast<size_t>(life_bits_words(static_cast<int>(W))) * static_cast<size_t>(H);
   if (pskel_status q = ensure_buffer(c->life_bits, 2 * plane * sizeof(uint32_t))) return q;
   uint32_t* A = static_cast<uint32_t*>(c->life_bits.ptr);
@@ -257,12 +257,15 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
                        true, c->err, c->sms, s);
   if (e != cudaSuccess) return cuda_fail(e, "Life pack launch");
   const std::vector<int> passes = plan_passes(iters, g.T);
-  for (size_t i = 0; i < passes.size(); ++i) {
-    const bool fwd = (i % 2 == 0);
-    e = life_bits_pass(fwd ? A : B, fwd ? B : A, static_cast<int>(W), static_cast<int>(H), ring, passes[i], g.T, g.TH,
-                       ctas, s);
-    if (e != cudaSuccess) return cuda_fail(e, "Life kernel launch");
-  }
+  // plan_passes: the first r passes have 2 more steps than the others (1 + 2q)
+  const int q = (passes.back() - 1) / 2;
+  int r = 0;
+  while (r < static_cast<int>(passes.size()) && passes[r] > passes.back()) ++r;
+  if (pskel_status qs = ensure_buffer(c->life_sync, life_bits_sync_bytes(static_cast<int>(W), static_cast<int>(H), g.TH)))
+    return qs;
+  e = life_bits_run_persistent(A, B, static_cast<int>(W), static_cast<int>(H), ring, static_cast<int>(passes.size()), q,
+                               r, g.T, g.TH, ctas, c->life_sync.ptr, c->err, s);
+  if (e != cudaSuccess) return cuda_fail(e, "Life kernel launch");
   // an odd number of passes (odd iterations) ends in B, whose result goes to `out`
   const bool odd = (passes.size() % 2) == 1;
   e = life_bits_unpack(odd ? B : A, static_cast<uint8_t*>(odd ? out : in), pitch, static_cast<int>(W),

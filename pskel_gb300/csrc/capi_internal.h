@@ -24,6 +24,7 @@ struct DeviceContext {
   DeviceBuffer partials;                           // 3D residual: per-CTA fp64 partial sums
   DeviceBuffer residuals;                          // 3D residual norms for *_host
   DeviceBuffer life_bits;                          // Life: the two bit planes of a run
+  DeviceBuffer life_sync;                          // Life: item counter and per-tile pass counts
 };
 
 pskel_status fail(pskel_status code, const char* fmt, ...);

@@ -36,6 +36,15 @@ cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch,
                              cudaStream_t s);
 cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
                            int ctas, cudaStream_t s);
+// Every pass in one persistent launch: pass i (of npasses) has
+// 1 + 2 * (q + (i < r)) steps and reads X (even i) or Y (odd i). Tiles wait
+// (bounded) for their neighbours' previous pass; `sync` holds the item
+// counter and per-tile completion counts (life_bits_sync_bytes, cleared here).
+// ctas must not exceed the resident CTAs (life_bits_persistent_ctas_per_sm).
+size_t life_bits_sync_bytes(int W, int H, int TH);
+int life_bits_persistent_ctas_per_sm();
+cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int ring, int npasses, int q, int r,
+                                     int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s);
 
 // ------------------------------------------------------- 2D float stencils
 

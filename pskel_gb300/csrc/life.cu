@@ -277,6 +277,125 @@ __global__ void __launch_bounds__(kBThreads, 2)
   }
 }
 
+constexpr unsigned kLifeSpinLimit = 1u << 24;  // polls of a neighbour's completion count (each with a sleep)
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Every pass of a run in one launch. Work items (pass, tile) are handed out
+// in order by an atomic counter; before tile t of pass p is staged, thread 0
+// waits (bounded) until every tile of pass p-1 whose core the tile reads --
+// rows within ceil(T/TH) tiles, one tile column either side -- has completed
+// (done[] counts the passes each tile has completed). Those tiles also were
+// the last readers of the region this tile writes. All CTAs are resident and
+// items are taken in order, so every awaited item is held by a running CTA.
+// Planes written by other SMs are read through L2 (ld.global.cg).
+// Pass i has 1 + 2 * (q + (i < r)) steps (the odd-length plan of
+// plan_passes).
+__global__ void __launch_bounds__(kBThreads, 2)
+    life_bits_persistent_kernel(uint32_t* __restrict__ planeX, uint32_t* __restrict__ planeY, int PW, int W, int H,
+                                int ring, int npasses, int q, int r, int T, int TH, int LH, int tiles_x, int tiles_y,
+                                unsigned long long* next_item, unsigned* done, unsigned* err) {
+  extern __shared__ __align__(128) uint32_t bsm[];
+  uint32_t* planeA = bsm;
+  uint32_t* planeB = bsm + kBPlane;
+  __shared__ long long s_item;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 2 * kBPlane; i += kBThreads) bsm[i] = 0u;
+  __syncthreads();
+  const int j = tid & (kBW - 1);
+  const int y0 = (tid / kBW) * kRowsPerStrip;
+  const int ntiles = tiles_x * tiles_y;
+  const long long nitems = static_cast<long long>(npasses) * ntiles;
+  const int dy = (T + TH - 1) / TH;
+  for (;;) {
+    if (tid == 0) s_item = static_cast<long long>(atomicAdd(next_item, 1ull));
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= nitems) break;
+    const int pass = static_cast<int>(item / ntiles);
+    const int tile = static_cast<int>(item - static_cast<long long>(pass) * ntiles);
+    const int steps = 1 + 2 * (q + (pass < r ? 1 : 0));
+    const uint32_t* src = (pass & 1) ? planeY : planeX;
+    uint32_t* dst = (pass & 1) ? planeX : planeY;
+    const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    int ok = 1;
+    if (tid == 0 && pass > 0) {
+      for (int yy = max(0, ty - dy); yy <= min(tiles_y - 1, ty + dy) && ok; ++yy) {
+        for (int xx = max(0, tx - 1); xx <= min(tiles_x - 1, tx + 1) && ok; ++xx) {
+          const unsigned* d = &done[yy * tiles_x + xx];
+          unsigned polls = 0;
+          while (ld_acquire_u32(d) < static_cast<unsigned>(pass)) {
+            if (++polls >= kLifeSpinLimit) {
+              atomicOr(err, kDevErrBarrier);
+              ok = 0;
+              break;
+            }
+            __nanosleep(32);
+          }
+        }
+      }
+    }
+    if (!__syncthreads_and(ok)) break;
+    __threadfence();
+    const int gy0 = ty * TH - T;
+    const int gw0 = tx * kBCore - 1;
+    const int gx0 = gw0 * 32;
+    const bool ring_tile = (gy0 < ring) || (gy0 + LH > H - ring) || (gx0 < ring) || (gx0 + kBW * 32 > W - ring);
+    const int nstage = ring_tile ? 2 : 1;
+    for (int k = 0; k < nstage; ++k) {
+      const uint32_t* g = (k == 0) ? src : dst;
+      uint32_t* pl = (k == 0) ? planeA : planeB;
+#pragma unroll 8
+      for (int i = tid; i < LH * kBW; i += kBThreads) {
+        const int row = i / kBW, wd = i - row * kBW;
+        const int gy = gy0 + row, gw = gw0 + wd;
+        const bool in = gy >= 0 && gy < H && gw >= 0 && gw < PW;
+        pl[(row + 1) * kBP + wd + 1] = in ? ld_cg(g + static_cast<int64_t>(gy) * PW + gw) : 0u;
+      }
+    }
+    for (int i = LH * kBW + tid; i < kBRows * kBW; i += kBThreads) {
+      const int row = i / kBW, wd = i - row * kBW;
+      planeA[(row + 1) * kBP + wd + 1] = 0u;
+      planeB[(row + 1) * kBP + wd + 1] = 0u;
+    }
+    __syncthreads();
+    const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
+    const bool active = y0 < LH;
+    for (int s = 0; s < steps; ++s) {
+      const uint32_t* in = (s & 1) ? planeB : planeA;
+      uint32_t* out = (s & 1) ? planeA : planeB;
+      if (active) {
+        if (ring_tile) {
+          life_strip<true, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+        } else {
+          life_strip<false, kBP>(in, out, y0, j, colmask, gy0, ring, H);
+        }
+      }
+      __syncthreads();
+    }
+    const uint32_t* fin = (steps & 1) ? planeB : planeA;
+    for (int i = tid; i < TH * kBCore; i += kBThreads) {
+      const int rr = i / kBCore, wd = 1 + (i - rr * kBCore);
+      const int row = T + rr;
+      const int gy = gy0 + row, gw = gw0 + wd;
+      if (gy < 0 || gy >= H || gw >= PW) continue;
+      dst[static_cast<int64_t>(gy) * PW + gw] = fin[(row + 1) * kBP + wd + 1];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicAdd(&done[tile], 1u);
+  }
+}
+
 }  // namespace
 
 int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
@@ -315,6 +434,35 @@ cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int
   const int tiles_y = (H + TH - 1) / TH;
   life_bits_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(src, dst, life_bits_words(W), W, H, ring, steps,
                                                                      T, TH, LH, tiles_x, tiles_y);
+  return cudaGetLastError();
+}
+
+size_t life_bits_sync_bytes(int W, int H, int TH) {
+  return 16 + sizeof(unsigned) * static_cast<size_t>(life_bits_tiles(W, H, TH));
+}
+
+int life_bits_persistent_ctas_per_sm() {
+  int n = 0;
+  const size_t smem = life_bits_smem_bytes();
+  cudaFuncSetAttribute(life_bits_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_persistent_kernel, kBThreads, smem) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int ring, int npasses, int q, int r,
+                                     int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s) {
+  const int LH = TH + 2 * T;
+  const int PW = life_bits_words(W);
+  const int tiles_x = (PW + kBCore - 1) / kBCore;
+  const int tiles_y = (H + TH - 1) / TH;
+  cudaError_t e = cudaMemsetAsync(sync, 0, life_bits_sync_bytes(W, H, TH), s);
+  if (e != cudaSuccess) return e;
+  unsigned long long* next = static_cast<unsigned long long*>(sync);
+  unsigned* done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
+  life_bits_persistent_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(
+      X, Y, PW, W, H, ring, npasses, q, r, T, TH, LH, tiles_x, tiles_y, next, done, err);
   return cudaGetLastError();
 }
 

@@ -236,10 +236,10 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
     if (!geom_for(sched->time_steps, g))
       return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", sched->time_steps);
   } else {
-    // Default: 15 generations per pass on full-height tiles (256 loaded rows)
-    // -- the fastest per generation on GB300 among 7..31 (measured: 13 and 21
-    // are 3-6 % slower, shorter tiles lose more to their fixed costs).
-    if (!geom_for(15, g) && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
+    // Default: 25 generations per pass on full-height tiles (256 loaded rows),
+    // the fastest measured on GB300 (8192^2: 22.4 T updates/s; 15: 21.0,
+    // 21: 21.9, 31: 21.4)
+    if (!geom_for(25, g) && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
   }
   const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), g.TH);
   // every pass in one persistent launch: no more CTAs than can be resident

@@ -28,14 +28,11 @@ std::vector<int> plan_passes(int64_t iters, int T);
 constexpr int kLifeBitsMaxT = 31;
 int life_bits_words(int W);
 size_t life_bits_smem_bytes();
-int life_bits_ctas_per_sm();
 int life_bits_tiles(int W, int H, int TH);
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
                            unsigned* err, int sms, cudaStream_t s);
 cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring, int sms,
                              cudaStream_t s);
-cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
-                           int ctas, cudaStream_t s);
 // Every pass in one persistent launch: pass i (of npasses) has
 // 1 + 2 * (q + (i < r)) steps and reads X (even i) or Y (odd i). Tiles wait
 // (bounded) for their neighbours' previous pass; `sync` holds the item

@@ -204,79 +204,6 @@ __device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src, bo
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// One pass of `steps` (<= T) generations from plane `src` to plane `dst`.
-__global__ void __launch_bounds__(kBThreads, 2)
-    life_bits_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int PW, int W, int H, int ring,
-                     int steps, int T, int TH, int LH, int tiles_x, int tiles_y) {
-  extern __shared__ __align__(128) uint32_t bsm[];
-  uint32_t* planeA = bsm;
-  uint32_t* planeB = bsm + kBPlane;
-  const int tid = threadIdx.x;
-  // the zero borders (row -1, row LH.., word -1, word 16) are never written
-  for (int i = tid; i < 2 * kBPlane; i += kBThreads) bsm[i] = 0u;
-  __syncthreads();
-  const int j = tid & (kBW - 1);
-  const int y0 = (tid / kBW) * kRowsPerStrip;
-  const int ntiles = tiles_x * tiles_y;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
-    const int gy0 = ty * TH - T;
-    const int gw0 = tx * kBCore - 1;
-    const int gx0 = gw0 * 32;
-    const bool ring_tile = (gy0 < ring) || (gy0 + LH > H - ring) || (gx0 < ring) || (gx0 + kBW * 32 > W - ring);
-    // ring tiles also stage the destination's tile: its ring bits are read by
-    // the odd steps and written back unchanged with the core words
-    const int nstage = ring_tile ? 2 : 1;
-    // stage the source tile (and, for ring tiles, the destination's) by cp.async
-    for (int k = 0; k < nstage; ++k) {
-      const uint32_t* g = (k == 0) ? src : dst;
-      uint32_t* pl = (k == 0) ? planeA : planeB;
-      for (int i = tid; i < LH * kBW; i += kBThreads) {
-        const int row = i / kBW, wd = i - row * kBW;
-        const int gy = gy0 + row, gw = gw0 + wd;
-        const bool ok = gy >= 0 && gy < H && gw >= 0 && gw < PW;
-        cp_async4(pl + (row + 1) * kBP + wd + 1, ok ? g + static_cast<int64_t>(gy) * PW + gw : g, ok);
-      }
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    // rows at or beyond LH stay zero from the last tile only if LH is the
-    // same; clear them (they feed only the halo, but keep them defined)
-    for (int i = LH * kBW + tid; i < kBRows * kBW; i += kBThreads) {
-      const int row = i / kBW, wd = i - row * kBW;
-      planeA[(row + 1) * kBP + wd + 1] = 0u;
-      planeB[(row + 1) * kBP + wd + 1] = 0u;
-    }
-    __syncthreads();
-    const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
-    // strips wholly below the loaded rows stay zero and are skipped: a tile
-    // costs its loaded height, not the plane's 256 rows
-    const bool active = y0 < LH;
-    for (int s = 0; s < steps; ++s) {
-      const uint32_t* in = (s & 1) ? planeB : planeA;
-      uint32_t* out = (s & 1) ? planeA : planeB;
-      if (active) {
-        if (ring_tile) {
-          life_strip<true, kBP>(in, out, y0, j, colmask, gy0, ring, H);
-        } else {
-          life_strip<false, kBP>(in, out, y0, j, colmask, gy0, ring, H);
-        }
-      }
-      __syncthreads();
-    }
-    // core words -> destination plane
-    const uint32_t* fin = (steps & 1) ? planeB : planeA;
-    for (int i = tid; i < TH * kBCore; i += kBThreads) {
-      const int r = i / kBCore, wd = 1 + (i - r * kBCore);
-      const int row = T + r;
-      const int gy = gy0 + row, gw = gw0 + wd;
-      if (gy < 0 || gy >= H || gw >= PW) continue;
-      dst[static_cast<int64_t>(gy) * PW + gw] = fin[(row + 1) * kBP + wd + 1];
-    }
-    __syncthreads();
-  }
-}
-
 constexpr unsigned kLifeSpinLimit = 1u << 24;  // polls of a neighbour's completion count (each with a sleep)
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -406,13 +333,6 @@ int life_bits_tiles(int W, int H, int TH) {
 
 size_t life_bits_smem_bytes() { return 2 * static_cast<size_t>(kBPlane) * sizeof(uint32_t); }
 
-int life_bits_ctas_per_sm() {
-  int n = 0;
-  const size_t smem = life_bits_smem_bytes();
-  cudaFuncSetAttribute(life_bits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_kernel, kBThreads, smem) != cudaSuccess) return 1;
-  return n > 0 ? n : 1;
-}
 
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
                            unsigned* err, int sms, cudaStream_t s) {
@@ -427,15 +347,6 @@ cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch,
   return cudaGetLastError();
 }
 
-cudaError_t life_bits_pass(const uint32_t* src, uint32_t* dst, int W, int H, int ring, int steps, int T, int TH,
-                           int ctas, cudaStream_t s) {
-  const int LH = TH + 2 * T;
-  const int tiles_x = (life_bits_words(W) + kBCore - 1) / kBCore;
-  const int tiles_y = (H + TH - 1) / TH;
-  life_bits_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(src, dst, life_bits_words(W), W, H, ring, steps,
-                                                                     T, TH, LH, tiles_x, tiles_y);
-  return cudaGetLastError();
-}
 
 size_t life_bits_sync_bytes(int W, int H, int TH) {
   return 16 + sizeof(unsigned) * static_cast<size_t>(life_bits_tiles(W, H, TH));

@@ -298,11 +298,17 @@ def run_ours(args, wl, world, rank, local):
 
     if is3d:
         passes = len(plan_any(iters, sch.time_steps))
+        launches = (passes + (iters // every if every else 0)) * args.steps  # + residual reductions
+    elif wl["name"] == "life":
+        # Life runs every pass in one persistent launch between two bit planes,
+        # plus two pack launches and one unpack launch
+        passes = 1
+        launches = 4 * args.steps
     else:
         passes = P.lib.pskel_plan_passes(iters, sch.time_steps, None, 0)
-    launches = passes * args.steps
+        launches = passes * args.steps
 
-    # kernel-only launch timing for the roofline: average pass duration
+    # kernel-only launch timing for the roofline: average pass (launch) duration
     per_launch_ms = sum(step_ms) / args.steps / passes
 
     # ---- end to end through the host entry point, pinned host buffers
@@ -358,6 +364,8 @@ def run_ours(args, wl, world, rank, local):
     b_alg = wl["b_alg"]
     achieved = b_alg * W * H * D * (iters / passes) / (per_launch_ms / 1e3) / 1e9
     pass_bytes = b_alg * W * H * D  # the pass's own compulsory traffic: read + write the grid once
+    if wl["name"] == "life":
+        pass_bytes = 3 * W * H  # HBM: pack reads both byte grids, unpack writes one; the bit planes stay in L2
     traffic = load_traffic(wl["name"])
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,

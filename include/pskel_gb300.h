@@ -268,6 +268,14 @@ PSKEL_API pskel_status pskel_mlp_destroy(pskel_mlp* m);
 /* Registers the model pskel_auto_schedule2d uses (NULL: the default schedule). */
 PSKEL_API pskel_status pskel_set_cost_model(pskel_mlp* m);
 
+/* Self-test of the kernels' bounded waits (no counterpart in the reference):
+ * launches a kernel that waits on an mbarrier phase that never completes
+ * (which = 0) or on a device flag that nothing sets (which = 1) for at most
+ * `polls` polls (1..2^20), then records the timeout in the device error word
+ * and returns. The next pskel_sync(stream) reports PSKEL_ERR_DEVICE (and
+ * clears it); the context stays usable. */
+PSKEL_API pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* stream);
+
 /* pskel_iterate3d without any allocation by the library. It has no
  * counterpart in the reference: it serves callers that cannot let a library
  * call cudaMalloc, such as a host application that owns all device memory

@@ -73,6 +73,7 @@ def _load():
     lib.pskel_iterate3d_noalloc.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                             C.c_int64, C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p,
                                             C.c_void_p]
+    lib.pskel_selftest_bounded_wait.argtypes = [C.c_int32, C.c_uint32, C.c_void_p]
     lib.pskel_run3d_host.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                      C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p]
     return lib

@@ -92,7 +92,7 @@ pskel_status device_sync_check(DeviceContext* c, cudaStream_t s) {
     std::string msg = "device error:";
     if (word & kDevErrTimeout) msg += " a TMA/mbarrier wait timed out;";
     if (word & kDevErrValue) msg += " a Life cell outside {0,1};";
-    if (word & kDevErrBarrier) msg += " a batched-schedule dependency wait timed out;";
+    if (word & kDevErrBarrier) msg += " a dependency wait between tiles or passes timed out;";
     if (word & kDevErrAlign) msg += " dynamic shared memory was not 128-byte aligned;";
     return fail(PSKEL_ERR_DEVICE, "%s", msg.c_str());
   }

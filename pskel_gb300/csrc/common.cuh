@@ -13,7 +13,7 @@ namespace pskel {
 enum DeviceError : unsigned {
   kDevErrTimeout = 1u,    // an mbarrier wait ran out of iterations
   kDevErrValue = 2u,      // an input value outside the kernel's domain (Life: cell not 0/1)
-  kDevErrBarrier = 4u,    // a batched-schedule dependency wait ran out of iterations
+  kDevErrBarrier = 4u,    // a dependency wait between tiles or passes ran out of iterations
   kDevErrAlign = 8u,      // dynamic shared memory not 128-byte aligned (kernel did nothing)
 };
 

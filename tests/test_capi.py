@@ -100,3 +100,11 @@ def test_pass_plan_parity():
             assert len(p) % 2 == iters % 2
             if iters >= T:
                 assert len(p) <= -(-iters // max(1, T - (T + 1) % 2)) + 1
+
+
+def test_selftest_rejects_bad_arguments():
+    # argument checks come before any device work
+    import pskel_gb300 as P
+    assert P.lib.pskel_selftest_bounded_wait(2, 10, None) == P.PSKEL_ERR_INVALID
+    assert P.lib.pskel_selftest_bounded_wait(0, 0, None) == P.PSKEL_ERR_INVALID
+    assert P.lib.pskel_selftest_bounded_wait(1, (1 << 20) + 1, None) == P.PSKEL_ERR_INVALID

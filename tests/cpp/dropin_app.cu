@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "PSkel.h"
+#include "PSkelMap.h"
 
 using namespace PSkel;
 
@@ -61,6 +62,17 @@ __parallel__ void stencilKernel(Array3D<float> in, Array3D<float> out, Mask3D<fl
 __parallel__ void stencilKernel(Array3D<float> in, Array3D<float> out, Mask3D<float> mask, HeatLib, size_t h, size_t w,
                                 size_t d) {
   stencilKernel(in, out, mask, HeatUser{0}, h, w, d);
+}
+// Map skeleton: an affine map out = a * in + b (product then sum, rounded each)
+struct Affine {
+  float a, b;
+};
+__parallel__ void mapKernel(Array<float> in, Array<float> out, Affine g, size_t i) { out(i) = g.a * in(i) + g.b; }
+__parallel__ void mapKernel(Array2D<float> in, Array2D<float> out, Affine g, size_t h, size_t w) {
+  out(h, w) = g.a * in(h, w) + g.b;
+}
+__parallel__ void mapKernel(Array3D<float> in, Array3D<float> out, Affine g, size_t h, size_t w, size_t d) {
+  out(h, w, d) = g.a * in(h, w, d) + g.b;
 }
 }  // namespace PSkel
 
@@ -152,6 +164,33 @@ int main(int argc, char** argv) {
       return 3;
     }
     write_raw(fres, out.hostArray, W * H);
+  } else if (sc.rfind("map", 0) == 0) {
+    const Affine g{0.75f, 0.125f};
+    const size_t n = W * H * D;
+    if (sc == "map1d_gpu" || sc == "map1d_seq") {
+      Array<float> in(n), out(n);
+      read_raw(fin, in.hostArray, n);
+      read_raw(fout, out.hostArray, n);
+      Map<Array<float>, Affine> m(in, out, g);
+      if (sc == "map1d_gpu") m.runIterativeGPU(it, 0); else m.runIterativeSequential(it);
+      write_raw(fres, out.hostArray, n);
+    } else if (sc == "map2d_gpu" || sc == "map2d_cpu") {
+      Array2D<float> in(W, H), out(W, H);
+      read_raw(fin, in.hostArray, n);
+      read_raw(fout, out.hostArray, n);
+      Map2D<Array2D<float>, Affine> m(in, out, g);
+      if (sc == "map2d_gpu") m.runIterativeGPU(it, 32); else m.runIterativeCPU(it, 4);
+      write_raw(fres, out.hostArray, n);
+    } else if (sc == "map3d_gpu") {
+      Array3D<float> in(W, H, D), out(W, H, D);
+      read_raw(fin, in.hostArray, n);
+      read_raw(fout, out.hostArray, n);
+      Map3D<Array3D<float>, Affine> m(in, out, g);
+      if (it == 1) m.runGPU(); else m.runIterativeGPU(it);
+      write_raw(fres, out.hostArray, n);
+    } else {
+      return 3;
+    }
   } else if (sc.rfind("heat", 0) == 0) {
     Array3D<float> in(W, H, D), out(W, H, D);
     read_raw(fin, in.hostArray, W * H * D);

@@ -6,8 +6,10 @@ functors). It is compiled here with nvcc against the drop-in headers and
 libpskel_gb300.so, run on seeded inputs, and its results are compared bit for
 bit with the oracle: library paths (tagged Args), user-functor paths (kernels
 generated from the functor, compiled with -fmad=false so the functor's sums
-are not contracted, as in the oracle), the schedule-taking overloads, and the
-host runIterativeCPU.
+are not contracted, as in the oracle), the schedule-taking overloads, the
+host runIterativeCPU, and the Map skeleton (include/PSkelMap.h). Host code is
+compiled with -ffp-contract=off: gcc on aarch64 contracts a*b+c into one
+fused multiply-add by default, which the oracle does not do.
 """
 from __future__ import annotations
 
@@ -35,7 +37,7 @@ def app():
     if not APP.exists() or APP.stat().st_mtime < max(APP_SRC.stat().st_mtime,
                                                       *(p.stat().st_mtime for p in (ROOT / "include").glob("*.h"))):
         cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-O2", "-fmad=false",
-               "-Xcompiler", "-fopenmp", "-DPSKEL_OMP", f"-I{ROOT / 'include'}", str(APP_SRC), "-o", str(APP),
+               "-Xcompiler", "-fopenmp,-ffp-contract=off", "-DPSKEL_OMP", f"-I{ROOT / 'include'}", str(APP_SRC), "-o", str(APP),
                f"-L{lib_dir}", "-lpskel_gb300", f"-Xlinker=-rpath,{lib_dir}", "-lgomp"]
         subprocess.run(cmd, check=True, capture_output=True)
     return APP
@@ -115,3 +117,23 @@ def test_dropin_auto_with_cost_model(app, oracle_mod, tmp_path):
         got, _ = run_app(app, "jacobi_auto", a, b, iters, env=env)
         want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def affine(x, iters):
+    # the app's mapKernel: out = 0.75 * in + 0.125, fp32 product then sum
+    a, b = np.float32(0.75), np.float32(0.125)
+    for _ in range(iters):
+        x = (a * x).astype(np.float32) + b
+    return x.astype(np.float32)
+
+
+@pytest.mark.parametrize("scenario", ["map1d_gpu", "map1d_seq", "map2d_gpu", "map2d_cpu", "map3d_gpu"])
+@pytest.mark.parametrize("iters", [1, 2, 5])
+def test_dropin_map(app, scenario, iters):
+    rng = np.random.default_rng(iters)
+    shape = (17, 33, 9) if scenario.startswith("map3d") else (61, 130)
+    a = rng.uniform(0, 1, shape).astype(np.float32)
+    b = rng.uniform(0, 1, shape).astype(np.float32)
+    a0 = a.copy()
+    got, _ = run_app(app, scenario, a, b, iters)
+    assert np.array_equal(got.view(np.uint32), affine(a0, iters).view(np.uint32))

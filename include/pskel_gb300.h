@@ -165,6 +165,40 @@ PSKEL_API pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_
                                         const pskel_schedule* sched, int64_t residual_every,
                                         double* residuals_host);
 
+/* ------------------------------------------------------------ out of core
+ * Grids kept in host memory and streamed through the GPU in slabs of whole
+ * rows (2D) or whole h-planes (3D), for grids larger than device memory.
+ * Replaces the host tiling of runIterativeTilingGPU / runTilingGPU /
+ * runAutoGPU (PSkelStencil.hpp:766-861, 1663-1760; tile geometry in
+ * PSkelStencilTiling.h:75-140). Each slab is copied to the device with a halo
+ * of ring + (T-1)*reach rows (2D) or T*reach planes (3D), iterated T =
+ * inner_iterations steps there (the last pass fewer) and its core copied back;
+ * copies in, compute and copies out of three consecutive slabs overlap on
+ * three streams. Results are those of pskel_run2d_host / pskel_run3d_host,
+ * bit for bit: `in_host` is not modified, the result lands in `out_host`
+ * (2D: `out_host` must hold the output array's initial ring, as for
+ * pskel_run2d_host). slab_rows = 0 sizes the slabs from `device_bytes`
+ * (0 = 90% of the free device memory); inner_iterations = 0 takes 15; an even
+ * inner_iterations is lowered by one. Host arrays that are not pinned are
+ * registered for the call; with two or more passes a pinned host array of the
+ * grid's size is allocated for the call. 3D: no residual norms. Synchronous. */
+PSKEL_API pskel_status pskel_run2d_host_tiled(const pskel_stencil* st, const void* in_host, void* out_host,
+                                              int64_t width, int64_t height, int64_t iterations, int64_t slab_rows,
+                                              int32_t inner_iterations, int64_t device_bytes,
+                                              const pskel_schedule* sched);
+PSKEL_API pskel_status pskel_run3d_host_tiled(const pskel_stencil* st, const void* in_host, void* out_host,
+                                              int64_t width, int64_t height, int64_t depth, int64_t iterations,
+                                              int64_t slab_planes, int32_t inner_iterations, int64_t device_bytes,
+                                              const pskel_schedule* sched);
+
+/* The slab plan the two calls above would use (host only unless both
+ * slab_rows and device_bytes are 0): plan[0] core rows per slab, plan[1] the
+ * widest halo (rows), plan[2] slabs per pass, plan[3] device bytes allocated.
+ * `depth` is ignored for a 2D mask. */
+PSKEL_API pskel_status pskel_tiled_plan(const pskel_stencil* st, int64_t width, int64_t height, int64_t depth,
+                                        int64_t iterations, int64_t slab_rows, int32_t inner_iterations,
+                                        int64_t device_bytes, int64_t plan[4]);
+
 /* ---------------------------------------------------------------- batches
  * Many 2D grids, each with its own size, iteration count and schedule, run by
  * ONE persistent kernel launch recorded once in a CUDA graph. There is no

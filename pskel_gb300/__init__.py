@@ -76,6 +76,12 @@ def _load():
     lib.pskel_selftest_bounded_wait.argtypes = [C.c_int32, C.c_uint32, C.c_void_p]
     lib.pskel_run3d_host.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                      C.c_int64, C.POINTER(Schedule), C.c_int64, C.c_void_p]
+    lib.pskel_run2d_host_tiled.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                           C.c_int64, C.c_int64, C.c_int32, C.c_int64, C.POINTER(Schedule)]
+    lib.pskel_run3d_host_tiled.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                           C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int64, C.POINTER(Schedule)]
+    lib.pskel_tiled_plan.argtypes = [C.POINTER(Stencil), C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                     C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
     return lib
 
 
@@ -181,6 +187,37 @@ def run3d_host(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int
     _check(lib.pskel_run3d_host(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, D, iterations,
                                 C.byref(sc) if sc is not None else None, residual_every, res.ctypes.data))
     return a_out, res[:n]
+
+
+def run2d_host_tiled(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int, slab_rows: int = 0,
+                     inner: int = 0, device_bytes: int = 0, sched=None):
+    """Out-of-core 2D run: slabs of rows streamed host -> device -> host; a_out is updated in place."""
+    assert a_in.flags.c_contiguous and a_out.flags.c_contiguous
+    H, W = a_in.shape
+    sc = make_schedule(sched)
+    _check(lib.pskel_run2d_host_tiled(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, iterations, slab_rows,
+                                      inner, device_bytes, C.byref(sc) if sc is not None else None))
+    return a_out
+
+
+def run3d_host_tiled(st: Stencil, a_in: np.ndarray, a_out: np.ndarray, iterations: int, slab_planes: int = 0,
+                     inner: int = 0, device_bytes: int = 0, sched=None):
+    """Out-of-core 3D run over h-plane slabs; arrays are [H][W][D]; a_out is updated in place."""
+    assert a_in.flags.c_contiguous and a_out.flags.c_contiguous
+    H, W, D = a_in.shape
+    sc = make_schedule(sched)
+    _check(lib.pskel_run3d_host_tiled(C.byref(st), a_in.ctypes.data, a_out.ctypes.data, W, H, D, iterations,
+                                      slab_planes, inner, device_bytes, C.byref(sc) if sc is not None else None))
+    return a_out
+
+
+def tiled_plan(st: Stencil, shape, iterations: int, slab_rows: int = 0, inner: int = 0, device_bytes: int = 0):
+    """(core rows per slab, halo rows, slabs per pass, device bytes) of an out-of-core run."""
+    H, W = shape[0], shape[1]
+    D = shape[2] if len(shape) == 3 else 1
+    out = (C.c_int64 * 4)()
+    _check(lib.pskel_tiled_plan(C.byref(st), W, H, D, iterations, slab_rows, inner, device_bytes, out))
+    return tuple(out)
 
 
 class Batch:

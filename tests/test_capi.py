@@ -108,3 +108,58 @@ def test_selftest_rejects_bad_arguments():
     assert P.lib.pskel_selftest_bounded_wait(2, 10, None) == P.PSKEL_ERR_INVALID
     assert P.lib.pskel_selftest_bounded_wait(0, 0, None) == P.PSKEL_ERR_INVALID
     assert P.lib.pskel_selftest_bounded_wait(1, (1 << 20) + 1, None) == P.PSKEL_ERR_INVALID
+
+
+def test_tiled_plan_arithmetic():
+    """Slab plan of the out-of-core calls (host only when a slab height or a
+    device budget is given): halo = ring + (T-1)*reach rows in 2D, T*reach
+    planes in 3D; three device slots of two buffers each, rows 128-byte
+    pitched in 2D, plus both arrays' ring columns."""
+    import pskel_gb300 as P
+    from pskel_gb300 import synth as S
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    # 21 steps in passes of at most 7: 7, 7, 7 (20 steps would be 5, 5, 5, 5)
+    assert P.tiled_plan(st, (500, 1000), 20, slab_rows=64, inner=7)[1] == 5
+    slab, halo, slabs, dev = P.tiled_plan(st, (500, 1000), 21, slab_rows=64, inner=7)
+    assert (slab, halo, slabs) == (64, 7, 8)
+    sub = 64 + 2 * 7
+    assert dev == 3 * 2 * (-(-sub * 4096 // 256) * 256) + 2 * (500 * 2 * 1 * 4)
+    # budget-sized: rows per slot from the budget, minus the halo on both sides
+    slab, halo, slabs, dev = P.tiled_plan(st, (500, 1000), 21, inner=7, device_bytes=4 << 20)
+    rows = ((4 << 20) - (2 * 4000 + (1 << 20))) // (3 * 2 * 4096 + 1000 // 4 + 64)
+    assert slab == rows - 2 * 7 and slabs == -(-500 // slab) and dev <= 4 << 20
+    # ring wider than the reach: halo = ring + (T-1)*reach
+    st3 = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, rng=3, keep=keep)
+    assert P.tiled_plan(st3, (500, 1000), 20, slab_rows=10, inner=5)[1] == 3 + 4
+    # even inner counts are lowered by one (odd pass lengths keep the ring parity)
+    assert P.tiled_plan(st, (500, 1000), 21, slab_rows=10, inner=8)[1] == 7
+    # 3D: T * reach planes, no ring columns
+    h3 = P.make_stencil(P.OP_LINEAR, "f32", S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, keep=keep)
+    slab, halo, slabs, dev = P.tiled_plan(h3, (57, 40, 72), 9, slab_rows=5, inner=3)
+    assert (slab, halo, slabs) == (5, 3, 12)
+    assert dev == 3 * 2 * (-(-(5 + 6) * 40 * 72 * 4 // 256) * 256)
+
+
+def test_tiled_rejects_bad_arguments():
+    import ctypes as C
+
+    import numpy as np
+
+    import pskel_gb300 as P
+    from pskel_gb300 import synth as S
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    a = np.zeros((40, 50), np.float32)
+    b = np.zeros((40, 50), np.float32)
+    f = P.lib.pskel_run2d_host_tiled
+    assert f(C.byref(st), None, b.ctypes.data, 50, 40, 3, 8, 3, 0, None) == P.PSKEL_ERR_INVALID
+    assert f(C.byref(st), a.ctypes.data, a.ctypes.data, 50, 40, 3, 8, 3, 0, None) == P.PSKEL_ERR_INVALID
+    assert f(C.byref(st), a.ctypes.data, b.ctypes.data, 50, 40, -1, 8, 3, 0, None) == P.PSKEL_ERR_INVALID
+    out = (C.c_int64 * 4)()
+    assert P.lib.pskel_tiled_plan(C.byref(st), 50, 40, 1, 3, -2, 3, 0, out) == P.PSKEL_ERR_INVALID
+    assert P.lib.pskel_tiled_plan(C.byref(st), 50, 40, 1, 3, 0, -1, 1 << 20, out) == P.PSKEL_ERR_INVALID
+    # a budget too small for one row plus its halo
+    assert P.lib.pskel_tiled_plan(C.byref(st), 50000, 40, 1, 30, 0, 15, 2 << 20, out) == P.PSKEL_ERR_NOMEM
+    life = P.make_stencil(P.OP_LIFE, "f32", S.MOORE8_OFFSETS, keep=keep)
+    assert P.lib.pskel_tiled_plan(C.byref(life), 50, 40, 1, 3, 8, 3, 0, out) == P.PSKEL_ERR_UNSUPPORTED

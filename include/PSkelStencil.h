@@ -47,6 +47,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -173,6 +174,21 @@ inline pskel_schedule make_schedule(size_t tw, size_t th, size_t td, size_t step
   return s;
 }
 
+// Device memory a run may use: the free memory, capped by the environment
+// variable PSKEL_DEVICE_BYTES when it is set (to run out of core on purpose).
+inline size_t device_budget() {
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    fr = 0;
+  }
+  if (const char* e = std::getenv("PSKEL_DEVICE_BYTES")) {
+    const unsigned long long cap = std::strtoull(e, nullptr, 10);
+    if (cap > 0 && (fr == 0 || cap < fr)) fr = static_cast<size_t>(cap);
+  }
+  return fr;
+}
+
 #ifdef __CUDACC__
 // ------------------------------------------------ user-functor GPU kernels
 
@@ -266,11 +282,27 @@ class StencilBase {
   Array output;
   Args args;
   Mask mask;
+  bool outOfCore = false;
 
   virtual void runGPUSchedule(size_t iterations, pskel_schedule sched) = 0;
 #ifdef PSKEL_OMP
   virtual void runOpenMP(Array in, Array out, size_t numThreads) = 0;
 #endif
+  // Device bytes an in-core run holds (the reference's test in runAutoGPU,
+  // PSkelStencil.hpp:832: input + output + mask below 99.8% of free memory).
+  virtual size_t inCoreBytes() { return input.memSize() + output.memSize() + 4096; }
+  bool fitsDevice(size_t budget) {
+    return budget == 0 || static_cast<double>(inCoreBytes()) < 0.998 * static_cast<double>(budget);
+  }
+  // Out-of-core run of a library stencil; false when there is none (user
+  // functors), and the caller then runs in core.
+  virtual bool runOutOfCore(size_t iterations, size_t slabRows, size_t innerIterations, size_t budget) {
+    (void)iterations;
+    (void)slabRows;
+    (void)innerIterations;
+    (void)budget;
+    return false;
+  }
 
  public:
   virtual ~StencilBase() {}
@@ -286,18 +318,30 @@ class StencilBase {
     (void)GPUBlockSizeY;
     runGPUSchedule(iterations, detail::make_schedule(0, 0, 0, pyramidHeight));
   }
+  // Arrays that fit in device memory run there, the tiling parameters sizing
+  // on-chip tiles; arrays that do not (the reference's reason for host tiles,
+  // PSkelStencil.hpp:829-861) run out of core: slabs of tilingHeight rows
+  // (h-planes in 3D) streamed through the device, innerIterations steps per
+  // visit.
   void runIterativeTilingGPU(size_t iterations, size_t tilingWidth, size_t tilingHeight, size_t tilingDepth,
                              size_t innerIterations = 1, size_t GPUBlockSizeX = 0, size_t GPUBlockSizeY = 0) {
     (void)GPUBlockSizeX;
     (void)GPUBlockSizeY;
-    runGPUSchedule(iterations, detail::make_schedule(tilingWidth, tilingHeight, tilingDepth, innerIterations));
+    const size_t budget = detail::device_budget();
+    outOfCore = !fitsDevice(budget) && runOutOfCore(iterations, tilingHeight, innerIterations, budget);
+    if (!outOfCore)
+      runGPUSchedule(iterations, detail::make_schedule(tilingWidth, tilingHeight, tilingDepth, innerIterations));
   }
   void runIterativeAutoGPU(size_t iterations, size_t GPUBlockSize = 0) {
     (void)GPUBlockSize;
-    runGPUSchedule(iterations, autoSchedule(iterations));
+    const size_t budget = detail::device_budget();
+    outOfCore = !fitsDevice(budget) && runOutOfCore(iterations, 0, 0, budget);
+    if (!outOfCore) runGPUSchedule(iterations, autoSchedule(iterations));
   }
   // An explicit schedule (a tuner's pick, for example).
   void runIterativeGPU(size_t iterations, const pskel_schedule& sched) { runGPUSchedule(iterations, sched); }
+  // Whether the last runIterativeTilingGPU / runIterativeAutoGPU ran out of core.
+  bool ranOutOfCore() const { return outOfCore; }
 
   void runGPU(size_t GPUBlockSizeX = 0, size_t GPUBlockSizeY = 0) { runIterativeGPU(1, GPUBlockSizeX, GPUBlockSizeY); }
   void runTilingGPU(size_t tilingWidth, size_t tilingHeight, size_t tilingDepth, size_t GPUBlockSizeX = 0,
@@ -378,7 +422,23 @@ class Stencil2D : public StencilBase<Array, Mask, Args> {
     }
   }
 
-  void runLibrary(size_t iterations, pskel_schedule sched) {
+  size_t inCoreBytes() override {
+    const size_t grid = this->input.memSize();
+    return (StencilOp<Args>::value == kAdvect ? 4 : 2) * grid + 4096;
+  }
+
+  bool runOutOfCore(size_t iterations, size_t slabRows, size_t innerIterations, size_t budget) override {
+    constexpr int op = StencilOp<Args>::value;
+    constexpr int dt = detail::LibDtype<T>::value;
+    if constexpr (op != kUserFunctor && dt >= 0) {
+      runLibrary(iterations, detail::make_schedule(0, 0, 0, 0), true, slabRows, innerIterations, budget);
+      return true;
+    }
+    return false;
+  }
+
+  void runLibrary(size_t iterations, pskel_schedule sched, bool tiled = false, size_t slabRows = 0,
+                  size_t innerIterations = 0, size_t budget = 0) {
     constexpr int op = StencilOp<Args>::value;
     std::vector<int32_t> off;
     std::vector<float> wt;
@@ -395,15 +455,23 @@ class Stencil2D : public StencilBase<Array, Mask, Args> {
       st.diffusivity = this->args.K;
       st.dt = this->args.dt;
       st.inv_dx = this->args.inv_dx;
-      pskelErrchk(pskel_run2d_host(&st, in.data(), out.data(), static_cast<int64_t>(this->input.getWidth()),
-                                   static_cast<int64_t>(this->input.getHeight()), static_cast<int64_t>(iterations),
-                                   &sched));
+      run2d(st, in.data(), out.data(), iterations, sched, tiled, slabRows, innerIterations, budget);
     } else {
-      pskelErrchk(pskel_run2d_host(&st, in.data(), out.data(), static_cast<int64_t>(this->input.getWidth()),
-                                   static_cast<int64_t>(this->input.getHeight()), static_cast<int64_t>(iterations),
-                                   &sched));
+      run2d(st, in.data(), out.data(), iterations, sched, tiled, slabRows, innerIterations, budget);
     }
     out.write_back();
+  }
+
+  void run2d(const pskel_stencil& st, const T* in, T* out, size_t iterations, const pskel_schedule& sched,
+             bool tiled, size_t slabRows, size_t innerIterations, size_t budget) {
+    const int64_t W = static_cast<int64_t>(this->input.getWidth()), H = static_cast<int64_t>(this->input.getHeight());
+    if (tiled) {
+      pskelErrchk(pskel_run2d_host_tiled(&st, in, out, W, H, static_cast<int64_t>(iterations),
+                                         static_cast<int64_t>(slabRows), static_cast<int32_t>(innerIterations),
+                                         static_cast<int64_t>(budget), nullptr));
+    } else {
+      pskelErrchk(pskel_run2d_host(&st, in, out, W, H, static_cast<int64_t>(iterations), &sched));
+    }
   }
 
   void runFunctor(size_t iterations, pskel_schedule sched) {
@@ -501,6 +569,36 @@ class Stencil3D : public StencilBase<Array, Mask, Args> {
  protected:
   size_t residualEvery = 0;
   std::vector<double> residualNorms;
+
+  // Out of core the residual norms are not recorded (residuals() is empty).
+  bool runOutOfCore(size_t iterations, size_t slabRows, size_t innerIterations, size_t budget) override {
+    constexpr int op = StencilOp<Args>::value;
+    constexpr int dt = detail::LibDtype<T>::value;
+    if constexpr (op == kLinear && dt >= 0 && dt != PSKEL_U8) {
+      std::vector<int32_t> off;
+      std::vector<float> wt;
+      pskel_stencil st;
+      std::memset(&st, 0, sizeof(st));
+      st.op = PSKEL_OP_LINEAR;
+      st.dtype = static_cast<pskel_dtype>(dt);
+      st.mask = detail::describe_mask(this->mask, off, wt);
+      detail::Contig<Array> in(this->input), out(this->output);
+      residualNorms.clear();
+      pskelErrchk(pskel_run3d_host_tiled(&st, in.data(), out.data(), static_cast<int64_t>(this->input.getWidth()),
+                                         static_cast<int64_t>(this->input.getHeight()),
+                                         static_cast<int64_t>(this->input.getDepth()),
+                                         static_cast<int64_t>(iterations), static_cast<int64_t>(slabRows),
+                                         static_cast<int32_t>(innerIterations), static_cast<int64_t>(budget),
+                                         nullptr));
+      out.write_back();
+      return true;
+    }
+    (void)iterations;
+    (void)slabRows;
+    (void)innerIterations;
+    (void)budget;
+    return false;
+  }
 
   void runGPUSchedule(size_t iterations, pskel_schedule sched) override {
     constexpr int op = StencilOp<Args>::value;

@@ -179,9 +179,11 @@ PSKEL_API pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_
  * (2D: `out_host` must hold the output array's initial ring, as for
  * pskel_run2d_host). slab_rows = 0 sizes the slabs from `device_bytes`
  * (0 = 90% of the free device memory); inner_iterations = 0 takes 15; an even
- * inner_iterations is lowered by one. Host arrays that are not pinned are
- * registered for the call; with two or more passes a pinned host array of the
- * grid's size is allocated for the call. 3D: no residual norms. Synchronous. */
+ * inner_iterations is lowered by one. The first pass reads `in_host`, later
+ * passes update `out_host` in place. Host arrays that are not pinned are
+ * registered for the call; the device slots (2 + ceil(halo/slab_rows), at
+ * least 3) stay allocated for later calls. 3D: no residual norms.
+ * Synchronous. */
 PSKEL_API pskel_status pskel_run2d_host_tiled(const pskel_stencil* st, const void* in_host, void* out_host,
                                               int64_t width, int64_t height, int64_t iterations, int64_t slab_rows,
                                               int32_t inner_iterations, int64_t device_bytes,

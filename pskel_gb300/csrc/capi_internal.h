@@ -25,6 +25,7 @@ struct DeviceContext {
   DeviceBuffer residuals;                          // 3D residual norms for *_host
   DeviceBuffer life_bits;                          // Life: the two bit planes of a run
   DeviceBuffer life_sync;                          // Life: item counter and per-tile pass counts
+  DeviceBuffer tiles;                              // out-of-core runs: slab slots and both arrays' rings
 };
 
 pskel_status fail(pskel_status code, const char* fmt, ...);

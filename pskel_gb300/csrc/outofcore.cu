@@ -10,10 +10,8 @@
 //
 // Here the tiles are full-width row slabs (whole h-planes in 3D): one slab is
 // one contiguous host range, so every copy is a single large DMA over C2C.
-// Three device slots rotate through H2D copy, compute and D2H copy on three
-// streams, so the copy engines (both directions) and the SMs work on three
-// consecutive slabs at once. A slab of the next pass waits only for the
-// write-backs of the slabs its rows come from.
+// Device slots rotate through H2D copy, compute and D2H copy on three streams,
+// so both copy directions and the SMs work on consecutive slabs at once.
 //
 // Each visit runs `T` steps on a sub-grid of the slab's rows plus a halo.
 // The sub-grid's edge rows that are not grid edges hold stale values (2D: the
@@ -22,18 +20,21 @@
 // steps it covers ring + (T-1)·R rows in 2D and T·R planes in 3D: those are
 // the halo widths, and the core rows come back exact.
 //
-// 2D ring semantics (each array keeps its own ring, the result sits in the
-// output array for odd iteration counts and in the input array for even ones)
-// are kept by giving every pass an odd length (pskel_plan_passes) and by
-// mapping the two logical arrays of the step-by-step run onto two physical
-// host arrays so that the last pass writes `out_host`: the physical array
-// standing for a logical one carries that array's ring. The ring columns of
-// both logical arrays are kept on the device for the whole run and scattered
-// into each slab's destination buffer by device copies.
+// One host array holds the state: the first pass reads `in_host` and writes
+// `out_host`, every later pass updates `out_host` in place. A slab's core is
+// written back only after every slab whose halo reads those rows has been
+// copied in (its "last reader"), so no pass reads a row that it already
+// advanced. 2D ring semantics (each array keeps its own ring; the result sits
+// in the output array for odd iteration counts and in the input array for
+// even ones) are kept by giving every pass an odd length (pskel_plan_passes)
+// and by keeping both arrays' rings on the device: each slab's destination
+// buffer gets the ring of the array the step-by-step run writes in that pass,
+// and the rows written back carry it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
+#include <deque>
 #include <vector>
 
 #include "capi_internal.h"
@@ -45,7 +46,6 @@ pskel_status validate2d(const pskel_stencil* st, const void* in, const void* out
 
 namespace {
 
-constexpr int kSlots = 3;
 constexpr int32_t kDefaultInner = 15;
 
 size_t dtype_bytes(pskel_dtype t) { return t == PSKEL_U8 ? 1 : (t == PSKEL_BF16 ? 2 : 4); }
@@ -99,20 +99,6 @@ struct Streams {
   }
 };
 
-struct DeviceAlloc {
-  void* ptr = nullptr;
-  ~DeviceAlloc() {
-    if (ptr) cudaFree(ptr);
-  }
-};
-
-struct PinnedAlloc {
-  void* ptr = nullptr;
-  ~PinnedAlloc() {
-    if (ptr) cudaFreeHost(ptr);
-  }
-};
-
 // One run's geometry: rows are h-rows (2D) or h-planes (3D).
 struct Plan {
   int dims = 2;
@@ -126,13 +112,26 @@ struct Plan {
   int64_t halo = 0;     // widest halo (rows), from the longest pass
   int64_t slab = 0;     // core rows per slab
   int64_t slabs = 0;
+  int slots = 3;        // device slots: 2 + the slabs a halo can span
   size_t slot_bytes = 0;
-  size_t ringcol_bytes = 0;  // 2D: ring columns of one logical array
+  size_t ringcol_bytes = 0;  // 2D: ring columns of one array (H rows x 2 ring)
+  size_t ringrow_bytes = 0;  // 2D: top and bottom ring rows of one array
   size_t device_bytes = 0;
 };
 
 int64_t halo_rows(const Plan& p, int T) {
   return p.dims == 2 ? p.ring + static_cast<int64_t>(T - 1) * p.R : static_cast<int64_t>(T) * p.R;
+}
+
+void size_plan(Plan& p, int64_t S) {
+  S = std::max<int64_t>(1, std::min<int64_t>(S, p.H));
+  p.slab = S;
+  p.slabs = (p.H + S - 1) / S;
+  p.slots = 2 + static_cast<int>(std::min<int64_t>(p.slabs, (p.halo + S - 1) / S));
+  p.slots = std::max(p.slots, 3);
+  const int64_t sub_max = std::min<int64_t>(p.H, S + 2 * p.halo);
+  p.slot_bytes = align_up(static_cast<size_t>(sub_max) * p.dev_row, 256);
+  p.device_bytes = static_cast<size_t>(p.slots) * p.fields * p.slot_bytes + 2 * (p.ringcol_bytes + p.ringrow_bytes);
 }
 
 pskel_status make_plan(Plan& p, int64_t iterations, int64_t slab_rows, int32_t inner, int64_t device_bytes) {
@@ -148,35 +147,35 @@ pskel_status make_plan(Plan& p, int64_t iterations, int64_t slab_rows, int32_t i
   int Tmax = 1;
   for (int t : p.passes) Tmax = std::max(Tmax, t);
   p.halo = halo_rows(p, Tmax);
-  p.ringcol_bytes = (p.dims == 2) ? static_cast<size_t>(p.H) * 2 * p.ring * p.esz : 0;
-  // Device memory besides the slots: ring columns of both logical arrays, and
-  // for Life the two bit planes and the pass counters of one sub-grid (about
-  // a quarter byte per cell).
-  const size_t fixed = 2 * p.ringcol_bytes + (1 << 20);
-  const size_t per_row = static_cast<size_t>(kSlots) * p.fields * p.dev_row + (p.dims == 2 ? p.W / 4 + 64 : 0);
-  int64_t S = slab_rows;
-  if (S == 0) {
-    size_t budget = static_cast<size_t>(device_bytes);
-    if (budget == 0) {
-      size_t fr = 0, tot = 0;
-      cudaError_t e = cudaMemGetInfo(&fr, &tot);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
-      budget = fr / 10 * 9;
-    }
-    if (budget <= fixed) return fail(PSKEL_ERR_NOMEM, "device budget %zu bytes is below the fixed need", budget);
-    const int64_t rows = static_cast<int64_t>((budget - fixed) / per_row);
-    S = rows - 2 * p.halo;
-    if (S < 1)
-      return fail(PSKEL_ERR_NOMEM,
-                  "device budget %zu bytes holds %lld rows per slot, fewer than a halo of %lld rows on each side",
-                  budget, (long long)rows, (long long)p.halo);
+  if (p.dims == 2) {
+    p.ringcol_bytes = align_up(static_cast<size_t>(p.H) * 2 * p.ring * p.esz, 256);
+    p.ringrow_bytes = align_up(2 * static_cast<size_t>(p.ring) * p.dev_row, 256);
   }
-  S = std::min<int64_t>(S, p.H);
-  p.slab = S;
-  p.slabs = (p.H + S - 1) / S;
-  const int64_t sub_max = std::min<int64_t>(p.H, S + 2 * p.halo);
-  p.slot_bytes = align_up(static_cast<size_t>(sub_max) * p.dev_row, 256);
-  p.device_bytes = static_cast<size_t>(kSlots) * p.fields * p.slot_bytes + 2 * p.ringcol_bytes;
+  if (slab_rows > 0) {
+    size_plan(p, slab_rows);
+    return PSKEL_OK;
+  }
+  size_t budget = static_cast<size_t>(device_bytes);
+  if (budget == 0) {
+    size_t fr = 0, tot = 0;
+    cudaError_t e = cudaMemGetInfo(&fr, &tot);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
+    budget = fr / 10 * 9;
+  }
+  // Device memory besides the slots: both arrays' rings, and for Life the two
+  // bit planes and pass counters of one sub-grid (a quarter byte per cell).
+  const size_t fixed = 2 * (p.ringcol_bytes + p.ringrow_bytes) + (1 << 20);
+  const size_t per_row = static_cast<size_t>(3) * p.fields * p.dev_row + (p.dims == 2 ? p.W / 4 + 64 : 0);
+  const int64_t rows = budget > fixed ? static_cast<int64_t>((budget - fixed) / per_row) : 0;
+  // three slots of slab + 2 halo rows, the slab no thinner than the halo
+  int64_t S = rows - 2 * p.halo;
+  if (S >= p.H) S = p.H;
+  if (S < std::min<int64_t>(p.halo, p.H) || S < 1)
+    return fail(PSKEL_ERR_NOMEM,
+                "device budget %zu bytes holds %lld rows per slot, too few for slabs of at least the halo (%lld rows) "
+                "with a halo on each side",
+                budget, (long long)rows, (long long)p.halo);
+  size_plan(p, S);
   return PSKEL_OK;
 }
 
@@ -196,22 +195,9 @@ cudaError_t rows_d2h(void* h, size_t row_bytes, const void* d, size_t dpitch, in
   return cudaMemcpy2DAsync(h, row_bytes, d, dpitch, row_bytes, static_cast<size_t>(rows), cudaMemcpyDeviceToHost, s);
 }
 
-// Host copy of the 2D ring cells (rows [0,r) and [H-r,H), columns [0,r) and
-// [W-r,W) of the rows between) from `src` to `dst`.
-void copy_ring_host(uint8_t* dst, const uint8_t* src, const Plan& p) {
-  const int64_t r = p.ring;
-  if (r == 0) return;
-  const size_t row = p.host_row;
-  const int64_t top = std::min<int64_t>(r, p.H);
-  std::memcpy(dst, src, row * static_cast<size_t>(top));
-  const int64_t bot0 = std::max<int64_t>(p.H - r, top);
-  std::memcpy(dst + row * bot0, src + row * bot0, row * static_cast<size_t>(p.H - bot0));
-  const size_t cw = static_cast<size_t>(std::min<int64_t>(r, p.W)) * p.esz;
-  const size_t off = static_cast<size_t>(p.W - std::min<int64_t>(r, p.W)) * p.esz;
-  for (int64_t y = top; y < bot0; ++y) {
-    std::memcpy(dst + row * y, src + row * y, cw);
-    std::memcpy(dst + row * y + off, src + row * y + off, cw);
-  }
+cudaError_t rows_d2d(void* d, const void* src, size_t pitch, size_t row_bytes, int64_t rows, cudaStream_t s) {
+  if (rows <= 0) return cudaSuccess;
+  return cudaMemcpy2DAsync(d, pitch, src, pitch, row_bytes, static_cast<size_t>(rows), cudaMemcpyDeviceToDevice, s);
 }
 
 struct Run {
@@ -220,8 +206,7 @@ struct Run {
   const pskel_schedule* sched = nullptr;
   const uint8_t* in = nullptr;  // in_host
   uint8_t* out = nullptr;       // out_host
-  uint8_t* scratch = nullptr;   // second physical array (pinned)
-  uint8_t* dev = nullptr;       // slots, then ring columns
+  uint8_t* dev = nullptr;       // slots, then ring columns and rows of both arrays
   DeviceContext* c = nullptr;
 };
 
@@ -229,23 +214,62 @@ uint8_t* slot_buf(const Run& r, int slot, int field) {
   return r.dev + (static_cast<size_t>(slot) * r.p.fields + field) * r.p.slot_bytes;
 }
 
-uint8_t* ringcols(const Run& r, int logical) {
-  return r.dev + static_cast<size_t>(kSlots) * r.p.fields * r.p.slot_bytes + logical * r.p.ringcol_bytes;
+// Ring columns (H rows x [left ring | right ring]) and ring rows (top ring
+// rows, then bottom ring rows, device pitch) of array L: 0 input, 1 output.
+uint8_t* ringcols(const Run& r, int L) {
+  return r.dev + static_cast<size_t>(r.p.slots) * r.p.fields * r.p.slot_bytes + L * r.p.ringcol_bytes;
 }
+uint8_t* ringrows(const Run& r, int L) {
+  return r.dev + static_cast<size_t>(r.p.slots) * r.p.fields * r.p.slot_bytes + 2 * r.p.ringcol_bytes +
+         L * r.p.ringrow_bytes;
+}
+
+// Copies both arrays' rings to the device (2D).
+cudaError_t stage_rings(const Run& r, cudaStream_t s) {
+  const Plan& p = r.p;
+  const size_t cw = static_cast<size_t>(p.ring) * p.esz;
+  const int64_t rr = std::min<int64_t>(p.ring, p.H);
+  for (int L = 0; L < 2; ++L) {
+    const uint8_t* src = (L == 0) ? r.in : r.out;
+    uint8_t* d = ringcols(r, L);
+    cudaError_t e =
+        cudaMemcpy2DAsync(d, 2 * cw, src, p.host_row, cw, static_cast<size_t>(p.H), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(d + cw, 2 * cw, src + (p.W - p.ring) * p.esz, p.host_row, cw, static_cast<size_t>(p.H),
+                            cudaMemcpyHostToDevice, s);
+    uint8_t* rw = ringrows(r, L);
+    if (e == cudaSuccess) e = rows_h2d(rw, p.dev_row, src, p.host_row, rr, s);
+    if (e == cudaSuccess)
+      e = rows_h2d(rw + p.dev_row * p.ring, p.dev_row, src + p.host_row * (p.H - rr), p.host_row, rr, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+struct Visit {
+  int64_t k;      // slab index within the pass
+  int slot;
+  int64_t y0, y1;  // core rows
+  int64_t a;       // first sub-grid row
+  int T;
+  int64_t last_reader;  // last slab of the pass whose sub-grid holds a core row
+};
 
 pskel_status run_slabs(Run& r) {
   const Plan& p = r.p;
   const int P = static_cast<int>(p.passes.size());
+  const int NS = p.slots;
   Streams ss;
   cudaError_t e = ss.create();
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
   cudaStream_t s_in = ss.s[0], s_comp = ss.s[1], s_out = ss.s[2];
-  cudaEvent_t ev_in[kSlots], ev_comp[kSlots], ev_free[kSlots];
-  for (int i = 0; i < kSlots; ++i) {
+  std::vector<cudaEvent_t> ev_in(NS), ev_comp(NS), ev_free(NS);
+  cudaEvent_t ev_loaded;  // recorded on s_in after each slab's copies in
+  for (int i = 0; i < NS; ++i)
     if ((e = ss.event(&ev_in[i])) != cudaSuccess || (e = ss.event(&ev_comp[i])) != cudaSuccess ||
         (e = ss.event(&ev_free[i])) != cudaSuccess)
       return cuda_fail(e, "cudaEventCreate");
-  }
+  if ((e = ss.event(&ev_loaded)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
   // ev_done[j % 2][k]: slab k of pass j written back to the host
   std::vector<cudaEvent_t> ev_done[2];
   for (auto& v : ev_done) {
@@ -253,67 +277,68 @@ pskel_status run_slabs(Run& r) {
     for (auto& x : v)
       if ((e = ss.event(&x)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
   }
-  std::vector<bool> slot_used(kSlots, false);
+  std::vector<bool> slot_used(static_cast<size_t>(NS), false);
+  if (p.dims == 2 && p.ring > 0 && (e = stage_rings(r, s_in)) != cudaSuccess)
+    return cuda_fail(e, "copy rings to device");
 
-  // Ring columns of both logical arrays on the device (2D): logical 0 is the
-  // input array, 1 the output array.
-  if (p.dims == 2 && p.ring > 0) {
-    const size_t cw = static_cast<size_t>(p.ring) * p.esz;
-    for (int L = 0; L < 2; ++L) {
-      const uint8_t* src = (L == 0) ? r.in : r.out;
-      uint8_t* d = ringcols(r, L);
-      e = cudaMemcpy2DAsync(d, 2 * cw, src, p.host_row, cw, static_cast<size_t>(p.H), cudaMemcpyHostToDevice, s_in);
-      if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(d + cw, 2 * cw, src + (p.W - p.ring) * p.esz, p.host_row, cw,
-                              static_cast<size_t>(p.H), cudaMemcpyHostToDevice, s_in);
-      if (e != cudaSuccess) return cuda_fail(e, "copy ring columns to device");
-    }
-    // The physical arrays take the rings of the logical arrays they stand for:
-    // out_host stands for the array holding the result (the output array for
-    // an odd count), the scratch array for the other one.
-    if (cudaStreamSynchronize(s_in) != cudaSuccess) return cuda_fail(cudaGetLastError(), "ring column copy");
-    const bool final_is_out = (P % 2 == 1);
-    if (P >= 2) copy_ring_host(r.scratch, final_is_out ? r.in : r.out, p);
-    if (!final_is_out) copy_ring_host(r.out, r.in, p);
-  }
+  std::deque<Visit> pending;  // computed, not yet written back
+  auto write_back = [&](const Visit& v, int j) -> pskel_status {
+    cudaError_t x = cudaStreamWaitEvent(s_out, ev_comp[v.slot], 0);
+    if (x == cudaSuccess) x = cudaStreamWaitEvent(s_out, ev_loaded, 0);
+    const uint8_t* res = (v.T % 2 == 1) ? slot_buf(r, v.slot, 1) : slot_buf(r, v.slot, 0);
+    if (x == cudaSuccess)
+      x = rows_d2h(r.out + p.host_row * v.y0, p.host_row, res + p.dev_row * (v.y0 - v.a), p.dev_row, v.y1 - v.y0,
+                   s_out);
+    if (x == cudaSuccess) x = cudaEventRecord(ev_free[v.slot], s_out);
+    if (x == cudaSuccess) x = cudaEventRecord(ev_done[j % 2][v.k], s_out);
+    return x == cudaSuccess ? PSKEL_OK : cuda_fail(x, "copy slab to host");
+  };
 
   int64_t visit = 0;
   for (int j = 0; j < P; ++j) {
     const int T = p.passes[static_cast<size_t>(j)];
     const int64_t halo = halo_rows(p, T);
-    const bool dst_is_out = ((P - 1 - j) % 2 == 0);
-    uint8_t* dst = dst_is_out ? r.out : r.scratch;
-    const uint8_t* src = (j == 0) ? r.in : (dst_is_out ? r.scratch : r.out);
-    const int logical_dst = (j % 2 == 0) ? 1 : 0;
+    const uint8_t* src = (j == 0) ? r.in : r.out;
+    const int Ldst = (j % 2 == 0) ? 1 : 0;  // the array step-by-step writes in this pass
     for (int64_t k = 0; k < p.slabs; ++k, ++visit) {
-      const int slot = static_cast<int>(visit % kSlots);
-      const int64_t y0 = k * p.slab, y1 = std::min(p.H, y0 + p.slab);
-      const int64_t a = std::max<int64_t>(0, y0 - halo), b = std::min<int64_t>(p.H, y1 + halo);
-      const int64_t hs = b - a;
-      uint8_t* dA = slot_buf(r, slot, 0);
-      uint8_t* dB = slot_buf(r, slot, 1);
-      // H2D: the slot is free once its previous slab was written back, and the
-      // source rows are final once the previous pass wrote them back.
-      if (slot_used[slot] && (e = cudaStreamWaitEvent(s_in, ev_free[slot], 0)) != cudaSuccess)
+      Visit v;
+      v.k = k;
+      v.slot = static_cast<int>(visit % NS);
+      v.y0 = k * p.slab;
+      v.y1 = std::min(p.H, v.y0 + p.slab);
+      v.a = std::max<int64_t>(0, v.y0 - halo);
+      v.T = T;
+      v.last_reader = std::min<int64_t>(p.slabs - 1, (v.y1 - 1 + halo) / p.slab);
+      const int64_t b = std::min<int64_t>(p.H, v.y1 + halo);
+      const int64_t hs = b - v.a;
+      uint8_t* dA = slot_buf(r, v.slot, 0);
+      uint8_t* dB = slot_buf(r, v.slot, 1);
+      // copies in: the slot is free once its previous slab was written back;
+      // the source rows are final once the previous pass wrote them back
+      if (slot_used[v.slot] && (e = cudaStreamWaitEvent(s_in, ev_free[v.slot], 0)) != cudaSuccess)
         return cuda_fail(e, "cudaStreamWaitEvent");
       if (j > 0) {
         const int64_t klast = std::min<int64_t>(p.slabs - 1, (b - 1) / p.slab);
         if ((e = cudaStreamWaitEvent(s_in, ev_done[(j - 1) % 2][klast], 0)) != cudaSuccess)
           return cuda_fail(e, "cudaStreamWaitEvent");
       }
-      e = rows_h2d(dA, p.dev_row, src + p.host_row * a, p.host_row, hs, s_in);
+      e = rows_h2d(dA, p.dev_row, src + p.host_row * v.a, p.host_row, hs, s_in);
       if (e == cudaSuccess && p.dims == 2 && p.ring > 0) {
+        // sub-grid ring: the destination array's own ring rows at a grid
+        // edge, the source rows elsewhere (any state works there), and the
+        // destination array's ring columns in between
         const int64_t rr = std::min<int64_t>(p.ring, hs);
-        // sub-grid ring rows: the destination array's own ring rows at a grid
-        // edge, any valid state (the source rows) elsewhere
-        e = rows_h2d(dB, p.dev_row, (a == 0 ? dst : src) + p.host_row * a, p.host_row, rr, s_in);
+        const size_t row = p.W * p.esz;
+        e = rows_d2d(dB, v.a == 0 ? ringrows(r, Ldst) : dA, p.dev_row, row, rr, s_in);
         if (e == cudaSuccess)
-          e = rows_h2d(dB + p.dev_row * (hs - rr), p.dev_row, (b == p.H ? dst : src) + p.host_row * (b - rr),
-                       p.host_row, rr, s_in);
+          e = rows_d2d(dB + p.dev_row * (hs - rr),
+                       b == p.H ? ringrows(r, Ldst) + p.dev_row * (p.ring - rr) + p.dev_row * p.ring
+                                : dA + p.dev_row * (hs - rr),
+                       p.dev_row, row, rr, s_in);
         const int64_t mid = hs - 2 * p.ring;
         if (e == cudaSuccess && mid > 0) {
           const size_t cw = static_cast<size_t>(p.ring) * p.esz;
-          const uint8_t* rc = ringcols(r, logical_dst) + static_cast<size_t>(a + p.ring) * 2 * cw;
+          const uint8_t* rc = ringcols(r, Ldst) + static_cast<size_t>(v.a + p.ring) * 2 * cw;
           e = cudaMemcpy2DAsync(dB + p.dev_row * p.ring, p.dev_row, rc, 2 * cw, cw, static_cast<size_t>(mid),
                                 cudaMemcpyDeviceToDevice, s_in);
           if (e == cudaSuccess)
@@ -322,39 +347,39 @@ pskel_status run_slabs(Run& r) {
         }
       }
       pskel_stencil sub = r.st;
-      if (e == cudaSuccess && p.dims == 2 && r.st.op == PSKEL_OP_ADVECT) {
-        uint8_t* dU = slot_buf(r, slot, 2);
-        uint8_t* dV = slot_buf(r, slot, 3);
-        e = rows_h2d(dU, p.dev_row, static_cast<const uint8_t*>(r.st.wind_u) + p.host_row * a, p.host_row, hs, s_in);
+      if (e == cudaSuccess && p.fields == 4) {
+        uint8_t* dU = slot_buf(r, v.slot, 2);
+        uint8_t* dV = slot_buf(r, v.slot, 3);
+        e = rows_h2d(dU, p.dev_row, static_cast<const uint8_t*>(r.st.wind_u) + p.host_row * v.a, p.host_row, hs,
+                     s_in);
         if (e == cudaSuccess)
-          e = rows_h2d(dV, p.dev_row, static_cast<const uint8_t*>(r.st.wind_v) + p.host_row * a, p.host_row, hs,
+          e = rows_h2d(dV, p.dev_row, static_cast<const uint8_t*>(r.st.wind_v) + p.host_row * v.a, p.host_row, hs,
                        s_in);
         sub.wind_u = dU;
         sub.wind_v = dV;
       }
+      if (e == cudaSuccess) e = cudaEventRecord(ev_in[v.slot], s_in);
+      if (e == cudaSuccess) e = cudaEventRecord(ev_loaded, s_in);
       if (e != cudaSuccess) return cuda_fail(e, "copy slab to device");
-      if ((e = cudaEventRecord(ev_in[slot], s_in)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
 
       // compute
-      if ((e = cudaStreamWaitEvent(s_comp, ev_in[slot], 0)) != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+      if ((e = cudaStreamWaitEvent(s_comp, ev_in[v.slot], 0)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamWaitEvent");
       pskel_status q;
       if (p.dims == 2)
         q = pskel_iterate2d(&sub, dA, dB, p.W, hs, static_cast<int64_t>(p.dev_row / p.esz), T, r.sched, s_comp);
       else
         q = pskel_iterate3d(&sub, dA, dB, p.W, hs, p.D, T, r.sched, 0, nullptr, s_comp);
       if (q != PSKEL_OK) return q;
-      if ((e = cudaEventRecord(ev_comp[slot], s_comp)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+      if ((e = cudaEventRecord(ev_comp[v.slot], s_comp)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+      slot_used[v.slot] = true;
 
-      // D2H of the core rows
-      if ((e = cudaStreamWaitEvent(s_out, ev_comp[slot], 0)) != cudaSuccess)
-        return cuda_fail(e, "cudaStreamWaitEvent");
-      const uint8_t* res = (T % 2 == 1) ? dB : dA;
-      e = rows_d2h(dst + p.host_row * y0, p.host_row, res + p.dev_row * (y0 - a), p.dev_row, y1 - y0, s_out);
-      if (e != cudaSuccess) return cuda_fail(e, "copy slab to host");
-      if ((e = cudaEventRecord(ev_free[slot], s_out)) != cudaSuccess ||
-          (e = cudaEventRecord(ev_done[j % 2][k], s_out)) != cudaSuccess)
-        return cuda_fail(e, "cudaEventRecord");
-      slot_used[slot] = true;
+      // write back every pending core whose last reader is now loaded
+      pending.push_back(v);
+      while (!pending.empty() && (pending.front().last_reader <= k || k == p.slabs - 1)) {
+        if (pskel_status w = write_back(pending.front(), j)) return w;
+        pending.pop_front();
+      }
     }
   }
   return device_sync_check(r.c, s_out);
@@ -376,19 +401,9 @@ pskel_status run_tiled(Run& r, int64_t iterations, int64_t slab_rows, int32_t in
     pin_u.pin(r.st.wind_u, grid_bytes);
     pin_v.pin(r.st.wind_v, grid_bytes);
   }
-  PinnedAlloc scratch;
-  if (p.passes.size() >= 2) {
-    cudaError_t e = cudaMallocHost(&scratch.ptr, grid_bytes);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost(out-of-core scratch array)");
-    r.scratch = static_cast<uint8_t*>(scratch.ptr);
-  }
-  DeviceAlloc dev;
-  cudaError_t e = cudaMalloc(&dev.ptr, p.device_bytes);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(out-of-core slots)");
-  r.dev = static_cast<uint8_t*>(dev.ptr);
-  pskel_status s = run_slabs(r);
-  cudaDeviceSynchronize();  // nothing in flight may touch the buffers freed below
-  return s;
+  if (pskel_status s = ensure_buffer(r.c->tiles, p.device_bytes)) return s;
+  r.dev = static_cast<uint8_t*>(r.c->tiles.ptr);
+  return run_slabs(r);
 }
 
 pskel_status fill_plan2d(const pskel_stencil* st, int64_t W, int64_t H, Plan& p) {

@@ -135,9 +135,11 @@ int main(int argc, char** argv) {
     } else if (sc == "jacobi_tiling") {
       Stencil2D<Array2D<float>, Mask2D<float>, JacobiLib> st(in, out, mask, JacobiLib());
       st.runIterativeTilingGPU(it, 64, 32, 1, 5);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
     } else if (sc == "jacobi_auto") {
       Stencil2D<Array2D<float>, Mask2D<float>, JacobiLib> st(in, out, mask, JacobiLib());
       st.runIterativeAutoGPU(it);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
     } else if (sc == "jacobi_user") {
       Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
       st.runIterativeGPU(it, 0, 0);
@@ -157,6 +159,10 @@ int main(int argc, char** argv) {
     if (sc == "life_lib") {
       Stencil2D<Array2D<uint8_t>, Mask2D<uint8_t>, LifeLib> st(in, out, mask, LifeLib());
       st.runIterativeGPU(it, 32, 4);
+    } else if (sc == "life_tiling") {
+      Stencil2D<Array2D<uint8_t>, Mask2D<uint8_t>, LifeLib> st(in, out, mask, LifeLib());
+      st.runIterativeTilingGPU(it, 0, 16, 1, 7);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
     } else if (sc == "life_user") {
       Stencil2D<Array2D<uint8_t>, Mask2D<uint8_t>, LifeUser> st(in, out, mask, LifeUser{0});
       st.runIterativeGPU(it, 7, 32, 4);
@@ -201,6 +207,10 @@ int main(int argc, char** argv) {
       st.setResidualInterval(2);
       st.runIterativeGPU(it, 0, 0);
       if (argc > 9) write_raw(argv[9], st.residuals().data(), st.residuals().size());
+    } else if (sc == "heat_tiling") {
+      Stencil3D<Array3D<float>, Mask3D<float>, HeatLib> st(in, out, mask, HeatLib());
+      st.runIterativeTilingGPU(it, W, 8, D, 3);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
     } else if (sc == "heat_user") {
       Stencil3D<Array3D<float>, Mask3D<float>, HeatUser> st(in, out, mask, HeatUser{0});
       st.runIterativeGPU(it, 0, 0);

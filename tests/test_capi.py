@@ -113,8 +113,9 @@ def test_selftest_rejects_bad_arguments():
 def test_tiled_plan_arithmetic():
     """Slab plan of the out-of-core calls (host only when a slab height or a
     device budget is given): halo = ring + (T-1)*reach rows in 2D, T*reach
-    planes in 3D; three device slots of two buffers each, rows 128-byte
-    pitched in 2D, plus both arrays' ring columns."""
+    planes in 3D; 2 + ceil(halo/slab) device slots (at least 3) of two
+    buffers each, rows 128-byte pitched in 2D, plus both arrays' ring columns
+    and ring rows."""
     import pskel_gb300 as P
     from pskel_gb300 import synth as S
     keep = P._Keep()
@@ -124,10 +125,16 @@ def test_tiled_plan_arithmetic():
     slab, halo, slabs, dev = P.tiled_plan(st, (500, 1000), 21, slab_rows=64, inner=7)
     assert (slab, halo, slabs) == (64, 7, 8)
     sub = 64 + 2 * 7
-    assert dev == 3 * 2 * (-(-sub * 4096 // 256) * 256) + 2 * (500 * 2 * 1 * 4)
+    up = lambda x: -(-x // 256) * 256  # noqa: E731
+    rings = 2 * (up(500 * 2 * 1 * 4) + up(2 * 1 * 4096))
+    assert dev == 3 * 2 * up(sub * 4096) + rings
+    # slabs thinner than the halo: one more slot per slab the halo spans
+    slab, halo, slabs, dev = P.tiled_plan(st, (500, 1000), 21, slab_rows=2, inner=7)
+    assert (slab, halo, slabs) == (2, 7, 250)
+    assert dev == (2 + 4) * 2 * up((2 + 14) * 4096) + rings
     # budget-sized: rows per slot from the budget, minus the halo on both sides
     slab, halo, slabs, dev = P.tiled_plan(st, (500, 1000), 21, inner=7, device_bytes=4 << 20)
-    rows = ((4 << 20) - (2 * 4000 + (1 << 20))) // (3 * 2 * 4096 + 1000 // 4 + 64)
+    rows = ((4 << 20) - (rings + (1 << 20))) // (3 * 2 * 4096 + 1000 // 4 + 64)
     assert slab == rows - 2 * 7 and slabs == -(-500 // slab) and dev <= 4 << 20
     # ring wider than the reach: halo = ring + (T-1)*reach
     st3 = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, rng=3, keep=keep)

@@ -21,6 +21,7 @@ import numpy as np
 import pytest
 
 from pskel_gb300 import synth as S
+from tests.gpu_util import bits
 
 pytestmark = pytest.mark.gpu
 
@@ -43,7 +44,7 @@ def app():
     return APP
 
 
-def run_app(app, scenario, a, b, iters, want_res=False, env=None):
+def run_app(app, scenario, a, b, iters, want_res=False, env=None, stdout=None):
     shape = a.shape
     H, W = shape[0], shape[1]
     D = shape[2] if len(shape) == 3 else 1
@@ -57,6 +58,8 @@ def run_app(app, scenario, a, b, iters, want_res=False, env=None):
             args.append(str(d / "norms"))
         r = subprocess.run(args, capture_output=True, text=True, env=env)
         assert r.returncode == 0, r.stderr
+        if stdout is not None:
+            stdout.append(r.stdout)
         res = np.fromfile(d / "res", dtype=a.dtype).reshape(shape)
         norms = np.fromfile(d / "norms", dtype=np.float64) if want_res else None
         return res, norms
@@ -137,3 +140,34 @@ def test_dropin_map(app, scenario, iters):
     a0 = a.copy()
     got, _ = run_app(app, scenario, a, b, iters)
     assert np.array_equal(got.view(np.uint32), affine(a0, iters).view(np.uint32))
+
+
+@pytest.mark.parametrize("scenario,shape,budget", [
+    ("jacobi_tiling", (157, 203), 200_000),   # slabs of tilingHeight = 32 rows, 5 steps per visit
+    ("jacobi_auto", (700, 520), 2 << 20),     # slabs sized from the budget
+    ("life_tiling", (227, 301), 100_000),
+    ("heat_tiling", (29, 37, 48), 300_000),   # slabs of 8 h-planes, 3 steps per visit
+])
+@pytest.mark.parametrize("iters", [1, 6, 13])
+def test_dropin_out_of_core(app, oracle_mod, scenario, shape, budget, iters):
+    """runIterativeTilingGPU / runIterativeAutoGPU on arrays larger than the
+    device memory the application may use (PSKEL_DEVICE_BYTES caps it) run out
+    of core, with the reference's results."""
+    import os
+    env = dict(os.environ, PSKEL_DEVICE_BYTES=str(budget))
+    if scenario.startswith("life"):
+        a, _ = S.life(shape[1], shape[0], seed=iters)
+        b = S.bernoulli_u8(iters + 7, S.S_GRID, a.shape, 0.5)
+        want = oracle_mod.life(a, b, iters)
+    elif scenario.startswith("heat"):
+        a, _ = S.heat3d(shape[1], shape[0], shape[2], seed=iters)
+        b = S.uniform_f32(iters + 3, S.S_GRID, a.shape)
+        want, _ = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, iters, halo=0.5)
+    else:
+        a, b = jac(shape[1], shape[0], iters)
+        want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters)
+    assert 2 * a.nbytes > budget
+    out = []
+    got, _ = run_app(app, scenario, a, b, iters, env=env, stdout=out)
+    assert "out of core" in out[0]
+    assert np.array_equal(bits(got), bits(want))

@@ -260,6 +260,14 @@ __global__ void __launch_bounds__(256) functor2d_pass(Array in, Array out, Mask 
   }
 }
 
+// One step of a user functor on a 1D array: every cell, grid-stride.
+template <class Array, class Mask, class Args>
+__global__ void __launch_bounds__(256) functor1d_step(Array in, Array out, Mask mask, Args args, size_t W) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < W;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    stencilKernel(in, out, mask, args, i);
+}
+
 // One step of a user functor on a 3D grid: every cell, d fastest across lanes.
 template <class Array, class Mask, class Args>
 __global__ void __launch_bounds__(128) functor3d_step(Array in, Array out, Mask mask, Args args, int W, int H, int D) {
@@ -542,6 +550,72 @@ class Stencil2D : public StencilBase<Array, Mask, Args> {
 #pragma omp parallel for num_threads(nt)
     for (long h = static_cast<long>(r); h < hr; ++h)
       for (size_t w = r; w + r < W; ++w) stencilKernel(in, out, this->mask, this->args, static_cast<size_t>(h), w);
+  }
+#endif
+};
+
+// ------------------------------------------------------------- Stencil (1D)
+
+// The 1D skeleton (PSkelStencil.h:384-407, PSkelStencil.hpp:2303-2327): every
+// cell i in [0, width) is updated each step by the user functor
+// stencilKernel(in, out, mask, args, i); Mask::get reads the halo value
+// outside the array. The GPU methods run one generated grid-stride kernel per
+// step, ping-ponging on the device; the result is copied into `output`.
+template <class Array, class Mask, class Args>
+class Stencil : public StencilBase<Array, Mask, Args> {
+ public:
+  Stencil() {}
+  Stencil(Array _input, Array _output, Mask _mask, Args _args) {
+    this->input = _input;
+    this->output = _output;
+    this->mask = _mask;
+    this->args = _args;
+  }
+
+ protected:
+  void runGPUSchedule(size_t iterations, pskel_schedule sched) override {
+    (void)sched;
+#ifdef __CUDACC__
+    const size_t W = this->input.getWidth();
+    Array in = this->input, out = this->output;
+    in.deviceAlloc();
+    out.deviceAlloc();
+    this->mask.deviceAlloc();
+    this->mask.copyToDevice();
+    in.copyToDevice();
+    int dev = 0, sms = 1;
+    gpuErrchk(cudaGetDevice(&dev));
+    gpuErrchk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    size_t blocks = (W + 255) / 256;
+    if (blocks > static_cast<size_t>(sms) * 8) blocks = static_cast<size_t>(sms) * 8;
+    if (blocks < 1) blocks = 1;
+    for (size_t it = 0; it < iterations; ++it) {
+      if (it % 2 == 0)
+        detail::functor1d_step<<<static_cast<unsigned>(blocks), 256>>>(in, out, this->mask, this->args, W);
+      else
+        detail::functor1d_step<<<static_cast<unsigned>(blocks), 256>>>(out, in, this->mask, this->args, W);
+      gpuErrchk(cudaPeekAtLastError());
+    }
+    gpuErrchk(cudaDeviceSynchronize());
+    if (iterations % 2 == 1)
+      this->output.copyFromDevice(out);
+    else
+      this->output.copyFromDevice(in);
+    in.deviceFree();
+    out.deviceFree();
+    this->mask.deviceFree();
+#else
+    (void)iterations;
+    static_assert(sizeof(Args) == 0, "the 1D stencil runs on the GPU only when this file is compiled with nvcc");
+#endif
+  }
+
+#ifdef PSKEL_OMP
+  void runOpenMP(Array in, Array out, size_t numThreads) override {
+    const long W = static_cast<long>(in.getWidth());
+    const int nt = numThreads ? static_cast<int>(numThreads) : omp_get_max_threads();
+#pragma omp parallel for num_threads(nt)
+    for (long i = 0; i < W; ++i) stencilKernel(in, out, this->mask, this->args, static_cast<size_t>(i));
   }
 #endif
 };

@@ -63,6 +63,15 @@ __parallel__ void stencilKernel(Array3D<float> in, Array3D<float> out, Mask3D<fl
                                 size_t d) {
   stencilKernel(in, out, mask, HeatUser{0}, h, w, d);
 }
+// 1D stencil: weighted sum over a 1D mask, halo value outside the array
+struct Smooth1D {
+  int unused;
+};
+__parallel__ void stencilKernel(Array<float> in, Array<float> out, Mask<float> mask, Smooth1D, size_t i) {
+  float acc = mask.getWeight(0) * mask.get(0, in, i);
+  for (size_t n = 1; n < mask.size; ++n) acc = acc + mask.getWeight(n) * mask.get(n, in, i);
+  out(i) = acc;
+}
 // Map skeleton: an affine map out = a * in + b (product then sum, rounded each)
 struct Affine {
   float a, b;
@@ -170,6 +179,23 @@ int main(int argc, char** argv) {
       return 3;
     }
     write_raw(fres, out.hostArray, W * H);
+  } else if (sc.rfind("stencil1d", 0) == 0) {
+    // 1D: W cells; mask offsets -2, -1, 0, 1, 3 with halo value 0.5
+    Array<float> in(W), out(W);
+    read_raw(fin, in.hostArray, W);
+    read_raw(fout, out.hostArray, W);
+    Mask<float> mask(5, 0.5f);
+    const int off[5] = {-2, -1, 0, 1, 3};
+    const float wt[5] = {0.125f, 0.25f, 0.3f, 0.2f, 0.125f};
+    for (int n = 0; n < 5; ++n) mask.set(n, off[n], wt[n]);
+    Stencil<Array<float>, Mask<float>, Smooth1D> st(in, out, mask, Smooth1D{0});
+    if (sc == "stencil1d_gpu")
+      st.runIterativeGPU(it, 0, 0);
+    else if (sc == "stencil1d_cpu")
+      st.runIterativeCPU(it, 4);
+    else
+      return 3;
+    write_raw(fres, out.hostArray, W);
   } else if (sc.rfind("map", 0) == 0) {
     const Affine g{0.75f, 0.125f};
     const size_t n = W * H * D;

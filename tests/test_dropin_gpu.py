@@ -171,3 +171,32 @@ def test_dropin_out_of_core(app, oracle_mod, scenario, shape, budget, iters):
     got, _ = run_app(app, scenario, a, b, iters, env=env, stdout=out)
     assert "out of core" in out[0]
     assert np.array_equal(bits(got), bits(want))
+
+
+def smooth1d(x, iters):
+    """The app's 1D stencil: sum_n w_n * in(i + o_n) in mask order, fp32,
+    the halo value 0.5 outside the array (Mask::get, PSkelMask.hpp:387-395)."""
+    off = [-2, -1, 0, 1, 3]
+    wt = [np.float32(v) for v in (0.125, 0.25, 0.3, 0.2, 0.125)]
+    x = x.astype(np.float32)
+    W = x.size
+    for _ in range(iters):
+        pad = np.full(W + 5, np.float32(0.5), dtype=np.float32)
+        pad[2:2 + W] = x
+        acc = None
+        for o, w in zip(off, wt):
+            term = (w * pad[2 + o:2 + o + W]).astype(np.float32)
+            acc = term if acc is None else (acc + term).astype(np.float32)
+        x = acc
+    return x
+
+
+@pytest.mark.parametrize("scenario", ["stencil1d_gpu", "stencil1d_cpu"])
+@pytest.mark.parametrize("W,iters", [(1, 1), (7, 2), (1000, 5), (100_003, 12)])
+def test_dropin_stencil1d(app, scenario, W, iters):
+    rng = np.random.default_rng(W + iters)
+    a = rng.uniform(0, 1, (1, W)).astype(np.float32)
+    b = rng.uniform(0, 1, (1, W)).astype(np.float32)
+    got, _ = run_app(app, scenario, a, b, iters)
+    want = smooth1d(a[0], iters)
+    assert np.array_equal(got[0].view(np.uint32), want.view(np.uint32))

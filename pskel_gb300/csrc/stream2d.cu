@@ -18,15 +18,18 @@ using fast2d::shape_of;
 // Rows are staged by TMA. A persistent block owns work items of 32 16-byte
 // vectors of columns (128 fp32 / 256 bf16 cells) x p.TH rows. A producer warp streams boxes of 8 rows (the row above
 // the group first) and 16 bytes of halo columns each side -- and, for
-// advection, the 8 rows of winds beside them -- into a ring of slots; eight
-// consumer warps compute the 8 rows of a group, one row each, reading the
-// three source rows from shared memory. Each slot has a "full" and an
-// "empty" mbarrier; every wait is bounded.
+// advection, the 8 rows of winds beside them -- into a ring of slots; the
+// consumer warps compute the 8 rows of a group, kRW consecutive rows each,
+// reading the kRW + 2 source rows once from shared memory and sharing their
+// conversions and neighbour shuffles between the rows. Each slot has a "full"
+// and an "empty" mbarrier; every wait is bounded.
 constexpr int kR2Slots = 5;
 constexpr int kR2Rows = 8;                    // rows per box and per group
 constexpr int kR2PhiBytes = (16 + 512 + 16) * kR2Rows;   // 4352
 constexpr int kR2WindBytes = 512 * kR2Rows;             // 4096
-constexpr int kR2Threads = 32 * (kR2Rows + 1);
+constexpr int kR2RW = 2;                      // rows per consumer warp
+constexpr int kR2Cons = kR2Rows / kR2RW;      // consumer warps
+constexpr int kR2Threads = 32 * (kR2Cons + 1);
 
 template <bool kAdvect>
 struct R2Slot {
@@ -61,7 +64,7 @@ __global__ void __launch_bounds__(kR2Threads, 3) stream2d_tma_kernel(const __gri
   if (tid == 0) {
     for (int i = 0; i < kR2Slots; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&empty[i], kR2Rows);
+      mbar_init(&empty[i], kR2Cons);
     }
     fence_barrier_init();
   }
@@ -79,7 +82,7 @@ __global__ void __launch_bounds__(kR2Threads, 3) stream2d_tma_kernel(const __gri
   };
   auto groups_of = [](int hs, int he) { return he > hs ? (he - hs + kR2Rows - 1) / kR2Rows : 0; };
 
-  if (warp == kR2Rows) {
+  if (warp == kR2Cons) {
     // ---- producer: boxes 0 .. groups of every item (box k: rows hs+8k-1 ..)
     if (lane == 0) {
       prefetch_tensormap(&map_phi);
@@ -116,7 +119,7 @@ __global__ void __launch_bounds__(kR2Threads, 3) stream2d_tma_kernel(const __gri
     return;
   }
 
-  // ---- consumers: warp w computes row hs + 8k + w of group k
+  // ---- consumers: warp w computes rows hs + 8k + kR2RW*w .. + kR2RW-1 of group k
   TS* __restrict__ dst = static_cast<TS*>(p.dst);
   const int64_t pitch = p.pitch;
   auto next = [](int s) { return s + 1 == kR2Slots ? 0 : s + 1; };
@@ -158,53 +161,53 @@ __global__ void __launch_bounds__(kR2Threads, 3) stream2d_tma_kernel(const __gri
         alive = false;
         break;
       }
-      const int r = hs + kR2Rows * k + warp;
-      Vt dn, cur, up;
-      float ldn, edn, lcur, ecur, lup, eup;
-      ld_row(s_a, s_b, warp, dn, ldn, edn);
-      ld_row(s_a, s_b, warp + 1, cur, lcur, ecur);
-      ld_row(s_a, s_b, warp + 2, up, lup, eup);
-      Vt uu, vv;
+      const int rbase = hs + kR2Rows * k + warp * kR2RW;
+      // staged rows rbase-1 .. rbase+kR2RW, with their west and east neighbours
+      Vt rows[kR2RW + 2];
+      float rw[kR2RW + 2], re[kR2RW + 2];
+#pragma unroll
+      for (int q = 0; q < kR2RW + 2; ++q) ld_row(s_a, s_b, warp * kR2RW + q, rows[q], rw[q], re[q]);
+      Vt uu[kR2RW], vv[kR2RW];
       if constexpr (kAdvect) {
-        const uint8_t* wrow = smem_raw + s_a * kStride + kR2PhiBytes + warp * 512 + lane * 16;
-        const uint4 a = *reinterpret_cast<const uint4*>(wrow);
-        const uint4 b = *reinterpret_cast<const uint4*>(wrow + kR2WindBytes);
-        uu.r[0] = a.x; uu.r[1] = a.y; uu.r[2] = a.z; uu.r[3] = a.w;
-        vv.r[0] = b.x; vv.r[1] = b.y; vv.r[2] = b.z; vv.r[3] = b.w;
+#pragma unroll
+        for (int j = 0; j < kR2RW; ++j) {
+          const uint8_t* wrow = smem_raw + s_a * kStride + kR2PhiBytes + (warp * kR2RW + j) * 512 + lane * 16;
+          const uint4 a = *reinterpret_cast<const uint4*>(wrow);
+          const uint4 b = *reinterpret_cast<const uint4*>(wrow + kR2WindBytes);
+          uu[j].r[0] = a.x; uu[j].r[1] = a.y; uu[j].r[2] = a.z; uu[j].r[3] = a.w;
+          vv[j].r[0] = b.x; vv[j].r[1] = b.y; vv[j].r[2] = b.z; vv[j].r[3] = b.w;
+        }
       }
       // box k (slot a) is done: group k-1 and this group were its readers
       __syncwarp();
       if (lane == 0) mbar_arrive1(&empty[s_a]);
-      float wd = __shfl_up_sync(0xFFFFFFFFu, dn.at(V - 1), 1), ed = __shfl_down_sync(0xFFFFFFFFu, dn.at(0), 1);
-      float wc = __shfl_up_sync(0xFFFFFFFFu, cur.at(V - 1), 1), ec = __shfl_down_sync(0xFFFFFFFFu, cur.at(0), 1);
-      float wup = __shfl_up_sync(0xFFFFFFFFu, up.at(V - 1), 1), eu = __shfl_down_sync(0xFFFFFFFFu, up.at(0), 1);
-      if (lane == 0) {
-        wd = ldn;
-        wc = lcur;
-        wup = lup;
+      float wq[kR2RW + 2], eq[kR2RW + 2];
+#pragma unroll
+      for (int q = 0; q < kR2RW + 2; ++q) {
+        wq[q] = __shfl_up_sync(0xFFFFFFFFu, rows[q].at(V - 1), 1);
+        eq[q] = __shfl_down_sync(0xFFFFFFFFu, rows[q].at(0), 1);
+        if (lane == 0) wq[q] = rw[q];
+        if (lane == 31) eq[q] = re[q];
       }
-      if (lane == 31) {
-        ed = edn;
-        ec = ecur;
-        eu = eup;
-      }
-      auto val = [&](const Vt& x, float west, float east, int kk) -> float {
-        return (kk < 0) ? west : (kk >= V ? east : x.at(kk));
+      auto val = [&](int q, int kk) -> float {
+        return (kk < 0) ? wq[q] : (kk >= V ? eq[q] : rows[q].at(kk));
       };
-      if (r < he && c_ok) {
+#pragma unroll
+      for (int j = 0; j < kR2RW; ++j) {
+        const int r = rbase + j;
+        if (!(r < he && c_ok)) continue;
         float res[V];
 #pragma unroll
         for (int kk = 0; kk < V; ++kk) {
           if constexpr (kAdvect) {
-            res[kk] = advect_cell(cur.at(kk), dn.at(kk), val(cur, wc, ec, kk + 1), val(cur, wc, ec, kk - 1),
-                                  up.at(kk), uu.at(kk), vv.at(kk), p.K, p.dt, p.inv_dx);
+            res[kk] = advect_cell(rows[j + 1].at(kk), rows[j].at(kk), val(j + 1, kk + 1), val(j + 1, kk - 1),
+                                  rows[j + 2].at(kk), uu[j].at(kk), vv[j].at(kk), p.K, p.dt, p.inv_dx);
           } else {
             float acc = 0.0f;
 #pragma unroll
             for (int n = 0; n < kTerms; ++n) {
               const int dh = shape_of<kShape>().dh[n], dw = shape_of<kShape>().dw[n];
-              const float x = (dh < 0) ? val(dn, wd, ed, kk + dw)
-                                       : (dh > 0 ? val(up, wup, eu, kk + dw) : val(cur, wc, ec, kk + dw));
+              const float x = val(j + 1 + dh, kk + dw);
               const float t = __fmul_rn(p.wt[n], x);
               acc = (n == 0) ? t : __fadd_rn(acc, t);
             }

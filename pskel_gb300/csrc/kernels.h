@@ -162,7 +162,7 @@ bool stream3d_is_cross7(const int* offsets, int n, int64_t D, int esize);
 // of 32 vectors of d x 16 w x p.HC planes); `map` is a 3D tensor map of the
 // source viewed as 32-bit words (dims D*esize/4, W, H; box 136 words x 18
 // rows x 1 plane). Residual partials: one per block.
-size_t stream3d_tma_smem_bytes();
+size_t stream3d_tma_smem_bytes(int dtype);
 int stream3d_tma_blocks_per_sm(int dtype);
 int64_t stream3d_tma_items(int W, int D, int hchunks, int esize);
 cudaError_t stream3d_tma_step(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas,

@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256)
 // cells) x 16 w rows x p.HC planes. A producer warp streams the planes h0-1 ..
 // h1 of its items, one 3D TMA copy per plane of the 34-vector x 18-row box
 // (a vector and a row of halo on each side; positions outside the grid are
-// zero-filled), into a ring of kS3Slots slots. Each slot has a "full"
+// zero-filled), into a ring of slots. Each slot has a "full"
 // mbarrier (the copy landed) and an "empty" one (all consumer warps have read
 // it), so consumer warps run independently of each other, up to the ring's
 // depth. Every wait is bounded. With a zero halo value the zero fill is the
@@ -342,18 +342,24 @@ __global__ void __launch_bounds__(256)
 // per warp convert and load each staged row fewer times per output cell, and
 // spread the per-plane waits over more cells: with 4 rows the issue-bound bf16
 // variant runs 8 % faster than with 2, the HBM-bound fp32 one the same.
-constexpr int kS3Slots = 6;
 constexpr int kS3BoxX = 34;                 // 16-byte vectors per staged row
 constexpr int kS3RowBytes = kS3BoxX * 16;   // 544
 constexpr int kS3BoxY = 18;                 // 16 rows + one each side
 constexpr int kS3PlaneBytes = (kS3RowBytes * kS3BoxY + 127) & ~127;
 constexpr int kS3MaxConsumers = 8;
 
+// Ring depth and residency per storage type, measured on GB300 (512^3 heat):
+// fp32 is HBM-bound and gains from a fourth resident block (4 slots, 4 blocks
+// per SM: 93 % of the measured copy bandwidth against 80 % with 6 slots and 3
+// blocks); bf16 is issue-bound and needs the registers of 3 blocks (6 slots).
 template <class TS>
 struct S3Rows {
-  static constexpr int kRW = 4;                      // w rows per consumer warp
-  static constexpr int kCons = 16 / kRW;               // consumer warps
-  static constexpr int kThreads = 32 * (kCons + 1);    // + the producer warp
+  static constexpr int kRW = 4;                            // w rows per consumer warp
+  static constexpr int kCons = 16 / kRW;                   // consumer warps
+  static constexpr int kThreads = 32 * (kCons + 1);        // + the producer warp
+  static constexpr int kSlots = sizeof(TS) == 4 ? 4 : 6;   // staged planes in the ring
+  static constexpr int kMinBlocks = sizeof(TS) == 4 ? 4 : 3;
+  static constexpr size_t kSmem = kSlots * static_cast<size_t>(kS3PlaneBytes) + 16 * kSlots;
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -367,13 +373,14 @@ __device__ __forceinline__ void consumers_sync() {
 }
 
 template <class TS, bool kReport, bool kZeroHalo>
-__global__ void __launch_bounds__(S3Rows<TS>::kThreads, 3)
+__global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
     stream3d_tma_kernel(const __grid_constant__ CUtensorMap map, const __grid_constant__ Stencil3DParams p) {
   using S = Storage<TS>;
   using Vt = Vec16<TS>;
   constexpr int V = Vt::V;
   constexpr int kRW = S3Rows<TS>::kRW;
   constexpr int kS3Consumers = S3Rows<TS>::kCons;
+  constexpr int kS3Slots = S3Rows<TS>::kSlots;
   extern __shared__ __align__(128) uint8_t smem_raw[];
   __shared__ double s_part[kS3MaxConsumers];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -672,11 +679,13 @@ int64_t stream3d_ctas(int W, int D, int hchunks) {
   return static_cast<int64_t>((D + 31) / 32) * ((W + 7) / 8) * hchunks;
 }
 
-size_t stream3d_tma_smem_bytes() { return kS3Slots * kS3PlaneBytes + 16 * kS3Slots; }
+size_t stream3d_tma_smem_bytes(int dtype) {
+  return dtype == 2 ? S3Rows<__nv_bfloat16>::kSmem : S3Rows<float>::kSmem;
+}
 
 template <class TS>
 int tma_blocks_per_sm() {
-  const size_t smem = stream3d_tma_smem_bytes();
+  const size_t smem = S3Rows<TS>::kSmem;
   void* ks[4] = {reinterpret_cast<void*>(stream3d_tma_kernel<TS, false, false>),
                  reinterpret_cast<void*>(stream3d_tma_kernel<TS, false, true>),
                  reinterpret_cast<void*>(stream3d_tma_kernel<TS, true, false>),
@@ -702,7 +711,7 @@ int64_t stream3d_tma_items(int W, int D, int hchunks, int esize) {
 
 template <class TS>
 void launch_tma(const CUtensorMap* map, const Stencil3DParams& p, int ctas, bool report, cudaStream_t s) {
-  const size_t smem = stream3d_tma_smem_bytes();
+  const size_t smem = S3Rows<TS>::kSmem;
   uint32_t hbits;
   std::memcpy(&hbits, &p.halo, sizeof(hbits));
   const bool zero = hbits == 0u;  // +0.0 exactly: the TMA zero fill is the halo

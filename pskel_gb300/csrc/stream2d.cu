@@ -23,7 +23,7 @@ using fast2d::shape_of;
 // reading the kRW + 2 source rows once from shared memory and sharing their
 // conversions and neighbour shuffles between the rows. Each slot has a "full"
 // and an "empty" mbarrier; every wait is bounded.
-constexpr int kR2Slots = 5;
+constexpr int kR2Slots = 4;
 constexpr int kR2Rows = 8;                    // rows per box and per group
 constexpr int kR2PhiBytes = (16 + 512 + 16) * kR2Rows;   // 4352
 constexpr int kR2WindBytes = 512 * kR2Rows;             // 4096
@@ -42,7 +42,7 @@ __device__ __forceinline__ void mbar_arrive1(uint64_t* bar) {
 }
 
 template <class TS, int OpK>
-__global__ void __launch_bounds__(kR2Threads, 3) stream2d_tma_kernel(const __grid_constant__ CUtensorMap map_phi,
+__global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __grid_constant__ CUtensorMap map_phi,
                                                                   const __grid_constant__ CUtensorMap map_u,
                                                                   const __grid_constant__ CUtensorMap map_v,
                                                                   const __grid_constant__ Stencil2DParams p) {

@@ -322,12 +322,13 @@ def run_ours(args, wl, world, rank, local):
         wind_host = (pu.data_ptr(), pv.data_ptr())
     st_h = stencil_for(wl, P, S, keep, wind_host)
     esz = pin_in.element_size()
+    r = 1  # ring of the 2D workloads (mask range 1)
     if is3d:
         h2d = W * H * D * esz  # the 3D output's initial contents are never read
         d2h = W * H * D * esz + 8 * (iters // every if every else 0)
     else:
         h2d = W * H * esz * (3 if "u" in x else 1)
-        r = 1  # the output array's ring goes to the device too (read by every second step)
+        # the output array's ring goes to the device too (read by every second step)
         h2d += (2 * r * W + 2 * r * (H - 2 * r)) * esz
         d2h = W * H * esz
     res_host = np.zeros(max(1, iters // every if every else 1), dtype=np.float64)
@@ -339,15 +340,27 @@ def run_ours(args, wl, world, rank, local):
         return P.lib.pskel_run2d_host(P.C.byref(st_h), pin_in.data_ptr(), pin_out.data_ptr(), W, H, iters,
                                       P.C.byref(sch))
 
+    def reset_out():
+        # Only what the call reads of the output array is restored between
+        # steps: its ring in 2D (the last run left the result's ring there),
+        # nothing in 3D (never read). Rewriting the whole pinned array from the
+        # CPU before each call would leave its lines dirty in the Grace caches
+        # and slow the device's coherent writes of the result into them.
+        if not is3d:
+            pin_out[:r].copy_(pin_out0[:r])
+            pin_out[-r:].copy_(pin_out0[-r:])
+            pin_out[:, :r].copy_(pin_out0[:, :r])
+            pin_out[:, -r:].copy_(pin_out0[:, -r:])
+
     def e2e_step():
-        pin_out.copy_(pin_out0)
+        reset_out()
         host_call()
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
     times = []
     for _ in range(args.steps):
-        pin_out.copy_(pin_out0)
+        reset_out()
         t1 = time.perf_counter()
         rc = host_call()
         times.append(time.perf_counter() - t1)

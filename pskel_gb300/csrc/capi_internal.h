@@ -20,9 +20,11 @@ struct DeviceContext {
   int smem_optin = 0;
   unsigned* err = nullptr;        // device error word (kernels atomicOr into it)
   cudaStream_t stream = nullptr;  // stream of the *_host entry points
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;  // their overlapped copies
   DeviceBuffer host_in, host_out, host_u, host_v;  // staging for *_host
   DeviceBuffer partials;                           // 3D residual: per-CTA fp64 partial sums
   DeviceBuffer residuals;                          // 3D residual norms for *_host
+  DeviceBuffer res_acc;                            // 3D wavefront: squared sums per reported step
   DeviceBuffer life_bits;                          // Life: the two bit planes of a run
   DeviceBuffer life_sync;                          // Life: item counter and per-tile pass counts
   DeviceBuffer tiles;                              // out-of-core runs: slab slots and both arrays' rings

@@ -146,6 +146,7 @@ struct Stencil3DParams {
   int every;           // report ||u_g - u_{g-1}|| when g % every == 0 (0: never)
   double* partials;    // scratch: steps x ctas fp64 partial sums
   double* residuals;   // device: one norm per reported step
+  int hbeg, hend;      // streaming 7-point kernel: planes [hbeg, hend) (hend 0: all)
 };
 
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize);
@@ -167,6 +168,13 @@ int stream3d_tma_blocks_per_sm(int dtype);
 int64_t stream3d_tma_items(int W, int D, int hchunks, int esize);
 cudaError_t stream3d_tma_step(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas,
                               cudaStream_t s);
+// One step of planes [p.hbeg, p.hend) with the streaming 7-point kernel; with
+// `acc` set the step's squared difference sum is added to *acc (one block,
+// fixed order) instead of written as a norm.
+cudaError_t stream3d_tma_band(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas, double* acc,
+                              cudaStream_t s);
+// residuals[i] = sqrt(acc[i]) for i < n.
+cudaError_t stream3d_finish_residuals(const double* acc, int n, double* residuals, cudaStream_t s);
 cudaError_t stencil3d_pass(int dtype, bool use_tma, const CUtensorMap* map_src, const Stencil3DParams& p, int ctas,
                            cudaStream_t s);
 

@@ -400,6 +400,7 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
   __syncthreads();
 
   const int H = p.H, W = p.W, D = p.D;
+  const int hbeg = p.hbeg, hend = p.hend > 0 ? p.hend : H;  // planes written by this launch
   const int dblocks = (D + 32 * V - 1) / (32 * V), wblocks = (W + 15) / 16;
   const int64_t items = static_cast<int64_t>(dblocks) * wblocks * p.hchunks;
   auto geometry = [&](int64_t it, int& d0, int& w0, int& h0, int& h1) {
@@ -407,8 +408,8 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
     const int64_t r = it / dblocks;
     d0 = db * 32 * V;
     w0 = static_cast<int>(r % wblocks) * 16;
-    h0 = static_cast<int>(r / wblocks) * p.HC;
-    h1 = min(H, h0 + p.HC);
+    h0 = hbeg + static_cast<int>(r / wblocks) * p.HC;
+    h1 = min(hend, h0 + p.HC);
   };
 
   if (warp == kS3Consumers) {
@@ -637,6 +638,24 @@ __global__ void reduce3d_residual(const double* __restrict__ partials, int nctas
   if (threadIdx.x == 0) residuals[(step0 + k) / every - 1] = sqrt(s[0]);
 }
 
+// Adds the CTA partials of one reported step to *acc (fixed order).
+__global__ void reduce3d_accumulate(const double* __restrict__ partials, int nctas, double* __restrict__ acc) {
+  __shared__ double s[256];
+  double t = 0.0;
+  for (int c = threadIdx.x; c < nctas; c += blockDim.x) t += partials[c];
+  s[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *acc += s[0];
+}
+
+__global__ void finish3d_residuals(const double* __restrict__ acc, int n, double* __restrict__ residuals) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) residuals[i] = sqrt(acc[i]);
+}
+
 template <class TS, int NM, bool kTma>
 cudaError_t launch3d(const CUtensorMap* map, const Stencil3DParams& p, int ctas, cudaStream_t s) {
   const size_t smem = stencil3d_smem_bytes(p.TW + 2 * p.HW, p.TD + 2 * p.HD, p.NP, p.T, sizeof(TS));
@@ -723,6 +742,24 @@ void launch_tma(const CUtensorMap* map, const Stencil3DParams& p, int ctas, bool
     stream3d_tma_kernel<TS, false, true><<<ctas, S3Rows<TS>::kThreads, smem, s>>>(*map, p);
   else
     stream3d_tma_kernel<TS, false, false><<<ctas, S3Rows<TS>::kThreads, smem, s>>>(*map, p);
+}
+
+cudaError_t stream3d_tma_band(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas, double* acc,
+                              cudaStream_t s) {
+  if (dtype == 2)
+    launch_tma<__nv_bfloat16>(map, p, ctas, acc != nullptr, s);
+  else
+    launch_tma<float>(map, p, ctas, acc != nullptr, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || acc == nullptr) return e;
+  reduce3d_accumulate<<<1, 256, 0, s>>>(p.partials, ctas, acc);
+  return cudaGetLastError();
+}
+
+cudaError_t stream3d_finish_residuals(const double* acc, int n, double* residuals, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  finish3d_residuals<<<(n + 255) / 256, 256, 0, s>>>(acc, n, residuals);
+  return cudaGetLastError();
 }
 
 cudaError_t stream3d_tma_step(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas,

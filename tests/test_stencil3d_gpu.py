@@ -145,3 +145,31 @@ def test_heat3d_c4_size_vs_oracle_and_fp64_error(cuda, oracle_mod):
     eb = float(np.max(np.abs(S.bf16_to_f32(gb) - ref64)))
     print(f"\nFP64-ERROR heat3d 128^3 x50: max abs fp32 {e32:.3e}, bf16 storage {eb:.3e}")
     assert e32 < 1e-5 and eb < 0.05
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H,D", [(40, 200, 64), (24, 128, 32), (17, 300, 16)])
+@pytest.mark.parametrize("iters,every", [(2, 0), (7, 3), (16, 4), (65, 13)])
+@pytest.mark.parametrize("halo", [0.0, 0.5])
+def test_host_run_wavefront(cuda, oracle_mod, dtype, W, H, D, iters, every, halo):
+    """pskel_run3d_host on grids of 128+ planes: chunks of planes are copied in
+    while earlier planes compute, and final planes go back while later ones
+    compute (a wavefront over the chunks). Same bits as the oracle; the fp64
+    residual norms within the stated tolerance."""
+    keep = P._Keep()
+    a, b = grids(W, H, D, W + H + D + iters, dtype)
+    st = heat(keep, dtype, halo=halo)
+    got, res = P.run3d_host(st, np.ascontiguousarray(a), np.ascontiguousarray(b).copy(), iters, residual_every=every)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, iters, halo=halo, dtype=dtype, every=every)
+    assert np.array_equal(bits(got), bits(want))
+    if every:
+        np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
+
+
+def test_host_run_wavefront_max_iterations(cuda, oracle_mod):
+    keep = P._Keep()
+    a, b = grids(32, 160, 32, 5, "f32")
+    got, res = P.run3d_host(heat(keep), a, b.copy(), 256, residual_every=64)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, 256, dtype="f32", every=64)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)

@@ -89,3 +89,48 @@ def test_batch_rejects_unsupported(cuda):
     with pytest.raises(P.PskelError) as ei:
         P.Batch(st, [(x, y, 3, 0)])
     assert ei.value.status == P.PSKEL_ERR_UNSUPPORTED
+
+
+def c5_shapes(n=256, seed=2025, smin=64, smax=2048, imin=10, imax=500):
+    """(W, H, iterations) of the batched workload's distribution: sides
+    log-uniform in [smin, smax], iterations uniform in [imin, imax]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        W = int(np.exp(rng.uniform(np.log(smin), np.log(smax))))
+        H = int(np.exp(rng.uniform(np.log(smin), np.log(smax))))
+        out.append((W, H, int(rng.integers(imin, imax + 1))))
+    return out
+
+
+def test_batch_full_distribution(cuda, oracle_mod):
+    """256 grids of the batched workload's distribution (670 MB of grids, more
+    than L2) in one launch, 7 steps per pass: the cell-update count, a replay
+    from the same inputs giving identical results, and the smallest grids
+    against the oracle."""
+    torch = cuda
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
+    grids = []
+    for i, (W, H, it) in enumerate(c5_shapes()):
+        pitch = aligned_pitch(W, 4)
+        a = S.uniform_f32(7, i, (H, W))
+        b = np.zeros_like(a)
+        x = to_dev(torch, a, pitch)
+        y = to_dev(torch, b, pitch)
+        grids.append(dict(a=a, b=b, W=W, H=H, it=it, pitch=pitch, x=x, y=y, x0=x.clone()))
+    batch = P.Batch(st, [(g["x"], g["y"], g["it"], 7, g["pitch"], g["W"]) for g in grids])
+    assert batch.cell_updates == sum(g["W"] * g["H"] * g["it"] for g in grids)
+    batch.run()
+    P.sync()
+    first = [result(g, "f32") for g in grids]
+    for g in grids:
+        g["x"].copy_(g["x0"])
+        g["y"].zero_()
+    batch.run()
+    P.sync()
+    assert all(np.array_equal(bits(result(g, "f32")), bits(f)) for g, f in zip(grids, first))
+    for g, got in sorted(zip(grids, first), key=lambda t: t[0]["W"] * t[0]["H"] * t[0]["it"])[:8]:
+        want = oracle_mod.lin2d(g["a"], g["b"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, g["it"])
+        assert np.array_equal(bits(got), bits(want)), (g["W"], g["H"], g["it"])
+    batch.close()

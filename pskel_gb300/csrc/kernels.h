@@ -39,6 +39,26 @@ cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch,
 // counter and per-tile completion counts (life_bits_sync_bytes, cleared here).
 // ctas must not exceed the resident CTAs (life_bits_persistent_ctas_per_sm).
 size_t life_bits_sync_bytes(int W, int H, int TH);
+// A launch's share of the passes of a run: passes pass0 .. pass0+np-1, each
+// over every tile, or (windowed) pass pass0+j over the tile rows
+// lo[j] .. lo[j] + (start[j+1]-start[j]) / tiles_x - 1 (start: prefix item
+// counts). Launches of one run share the completion counts, so a tile waits
+// for its neighbourhood's previous pass whichever launch ran it.
+constexpr int kLifeMaxWindow = 16;
+struct LifeWindow {
+  int pass0, np, windowed;
+  int lo[kLifeMaxWindow];
+  long long start[kLifeMaxWindow + 1];
+};
+cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t s);
+cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int ring, const LifeWindow& win, int q,
+                                 int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s);
+// Pack rows [row0, row1) (every cell checked to be 0/1) / unpack the interior
+// cells of rows [row0, row1).
+cudaError_t life_bits_pack_rows(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring,
+                                int row0, int row1, unsigned* err, int sms, cudaStream_t s);
+cudaError_t life_bits_unpack_rows(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring,
+                                  int row0, int row1, int sms, cudaStream_t s);
 int life_bits_persistent_ctas_per_sm();
 cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int ring, int npasses, int q, int r,
                                      int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s);

@@ -135,12 +135,13 @@ constexpr int kBThreads = kBW * (kBRows / kRowsPerStrip);  // 512: a word column
 // before it is read)
 __global__ void __launch_bounds__(256) life_pack_kernel(const uint8_t* __restrict__ src, int64_t pitch, int W, int H,
                                                         uint32_t* __restrict__ plane, int PW, int ring, int check,
-                                                        unsigned* err) {
+                                                        unsigned* err, int row0, int row1) {
   bool bad = false;
-  const int64_t n = static_cast<int64_t>(H) * PW;
+  const int64_t n = static_cast<int64_t>(row1 - row0) * PW;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int row = static_cast<int>(i / PW), wd = static_cast<int>(i - static_cast<int64_t>(row) * PW);
+    const int rr = static_cast<int>(i / PW), wd = static_cast<int>(i - static_cast<int64_t>(rr) * PW);
+    const int row = row0 + rr;
     const int c0 = wd * 32;
     const uint8_t* r = src + static_cast<int64_t>(row) * pitch;
     const bool row_ring = row < ring || row >= H - ring;
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(256) life_pack_kernel(const uint8_t* __restric
         bits |= static_cast<uint32_t>(v & 1u) << k;
       }
     }
-    plane[i] = bits;
+    plane[static_cast<int64_t>(row) * PW + wd] = bits;
   }
   if (bad) atomicOr(err, kDevErrValue);
 }
@@ -175,13 +176,16 @@ __global__ void __launch_bounds__(256) life_pack_kernel(const uint8_t* __restric
 // writes the interior cells (ring <= h < H-ring, ring <= w < W-ring) of a bit
 // plane into `dst` as bytes; ring cells of `dst` are left as they are
 __global__ void __launch_bounds__(256) life_unpack_kernel(const uint32_t* __restrict__ plane, int PW, uint8_t* dst,
-                                                          int64_t pitch, int W, int H, int ring) {
-  const int rows = H - 2 * ring;
+                                                          int64_t pitch, int W, int H, int ring, int row0,
+                                                          int row1) {
+  // interior rows of [row0, row1)
+  const int lo = max(ring, row0), hi = min(H - ring, row1);
+  const int rows = hi - lo;
   if (rows <= 0) return;
   const int64_t n = static_cast<int64_t>(rows) * PW;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int row = ring + static_cast<int>(i / PW), wd = static_cast<int>(i % PW);
+    const int row = lo + static_cast<int>(i / PW), wd = static_cast<int>(i % PW);
     const int c0 = wd * 32;
     if (c0 >= W - ring || c0 + 32 <= ring) continue;
     const uint32_t bits = plane[static_cast<int64_t>(row) * PW + wd];
@@ -197,12 +201,6 @@ __global__ void __launch_bounds__(256) life_unpack_kernel(const uint32_t* __rest
     }
   }
 }
-
-__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src, bool valid) {
-  const int n = valid ? 4 : 0;  // zero-fill when the source word lies outside the plane
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(n) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 constexpr unsigned kLifeSpinLimit = 1u << 24;  // polls of a neighbour's completion count (each with a sleep)
 
@@ -230,26 +228,47 @@ __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) {
 __global__ void __launch_bounds__(kBThreads, 2)
     life_bits_persistent_kernel(uint32_t* __restrict__ planeX, uint32_t* __restrict__ planeY, int PW, int W, int H,
                                 int ring, int npasses, int q, int r, int T, int TH, int LH, int tiles_x, int tiles_y,
-                                unsigned long long* next_item, unsigned* done, unsigned* err) {
+                                unsigned long long* next_item, unsigned* done, unsigned* err,
+                                const __grid_constant__ LifeWindow win) {
   extern __shared__ __align__(128) uint32_t bsm[];
   uint32_t* planeA = bsm;
   uint32_t* planeB = bsm + kBPlane;
   __shared__ long long s_item;
+  __shared__ int s_pass, s_tile;
+  (void)npasses;
   const int tid = threadIdx.x;
   for (int i = tid; i < 2 * kBPlane; i += kBThreads) bsm[i] = 0u;
   __syncthreads();
   const int j = tid & (kBW - 1);
   const int y0 = (tid / kBW) * kRowsPerStrip;
   const int ntiles = tiles_x * tiles_y;
-  const long long nitems = static_cast<long long>(npasses) * ntiles;
+  // this launch's items: passes win.pass0 .. + win.np, each over all tiles or
+  // (windowed) over tile rows [win.lo[j], ...) holding win.start[j+1] -
+  // win.start[j] items; completion counts persist between the launches of a run
+  const long long nitems = win.windowed ? win.start[win.np] : static_cast<long long>(win.np) * ntiles;
   const int dy = (T + TH - 1) / TH;
   for (;;) {
-    if (tid == 0) s_item = static_cast<long long>(atomicAdd(next_item, 1ull));
+    if (tid == 0) {
+      const long long it = static_cast<long long>(atomicAdd(next_item, 1ull));
+      s_item = it;
+      if (it < nitems) {
+        if (win.windowed) {
+          int j = 0;
+          while (j + 1 < win.np && win.start[j + 1] <= it) ++j;
+          const long long k = it - win.start[j];
+          s_pass = win.pass0 + j;
+          s_tile = static_cast<int>((win.lo[j] + k / tiles_x) * tiles_x + k % tiles_x);
+        } else {
+          s_pass = win.pass0 + static_cast<int>(it / ntiles);
+          s_tile = static_cast<int>(it % ntiles);
+        }
+      }
+    }
     __syncthreads();
     const long long item = s_item;
     if (item >= nitems) break;
-    const int pass = static_cast<int>(item / ntiles);
-    const int tile = static_cast<int>(item - static_cast<long long>(pass) * ntiles);
+    const int pass = s_pass;
+    const int tile = s_tile;
     const int steps = 1 + 2 * (q + (pass < r ? 1 : 0));
     const uint32_t* src = (pass & 1) ? planeY : planeX;
     uint32_t* dst = (pass & 1) ? planeX : planeY;
@@ -337,13 +356,28 @@ size_t life_bits_smem_bytes() { return 2 * static_cast<size_t>(kBPlane) * sizeof
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
                            unsigned* err, int sms, cudaStream_t s) {
   const int PW = life_bits_words(W);
-  life_pack_kernel<<<4 * sms, 256, 0, s>>>(src, pitch, W, H, plane, PW, ring, ring_only ? 1 : 0, err);
+  life_pack_kernel<<<4 * sms, 256, 0, s>>>(src, pitch, W, H, plane, PW, ring, ring_only ? 1 : 0, err, 0, H);
+  return cudaGetLastError();
+}
+
+cudaError_t life_bits_pack_rows(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring,
+                                int row0, int row1, unsigned* err, int sms, cudaStream_t s) {
+  if (row1 <= row0) return cudaSuccess;
+  const int PW = life_bits_words(W);
+  life_pack_kernel<<<4 * sms, 256, 0, s>>>(src, pitch, W, H, plane, PW, ring, 0, err, row0, row1);
   return cudaGetLastError();
 }
 
 cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring, int sms,
                              cudaStream_t s) {
-  life_unpack_kernel<<<4 * sms, 256, 0, s>>>(plane, life_bits_words(W), dst, pitch, W, H, ring);
+  life_unpack_kernel<<<4 * sms, 256, 0, s>>>(plane, life_bits_words(W), dst, pitch, W, H, ring, 0, H);
+  return cudaGetLastError();
+}
+
+cudaError_t life_bits_unpack_rows(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring,
+                                  int row0, int row1, int sms, cudaStream_t s) {
+  if (row1 <= row0) return cudaSuccess;
+  life_unpack_kernel<<<4 * sms, 256, 0, s>>>(plane, life_bits_words(W), dst, pitch, W, H, ring, row0, row1);
   return cudaGetLastError();
 }
 
@@ -372,8 +406,31 @@ cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int
   if (e != cudaSuccess) return e;
   unsigned long long* next = static_cast<unsigned long long*>(sync);
   unsigned* done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
+  LifeWindow win;
+  memset(&win, 0, sizeof(win));
+  win.np = npasses;
   life_bits_persistent_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(
-      X, Y, PW, W, H, ring, npasses, q, r, T, TH, LH, tiles_x, tiles_y, next, done, err);
+      X, Y, PW, W, H, ring, npasses, q, r, T, TH, LH, tiles_x, tiles_y, next, done, err, win);
+  return cudaGetLastError();
+}
+
+cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t s) {
+  return cudaMemsetAsync(sync, 0, life_bits_sync_bytes(W, H, TH), s);
+}
+
+cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int ring, const LifeWindow& win, int q,
+                                 int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s) {
+  const int LH = TH + 2 * T;
+  const int PW = life_bits_words(W);
+  const int tiles_x = (PW + kBCore - 1) / kBCore;
+  const int tiles_y = (H + TH - 1) / TH;
+  // the item counter restarts; the per-tile completion counts carry over
+  cudaError_t e = cudaMemsetAsync(sync, 0, 16, s);
+  if (e != cudaSuccess) return e;
+  unsigned long long* next = static_cast<unsigned long long*>(sync);
+  unsigned* done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
+  life_bits_persistent_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(
+      X, Y, PW, W, H, ring, win.pass0 + win.np, q, r, T, TH, LH, tiles_x, tiles_y, next, done, err, win);
   return cudaGetLastError();
 }
 

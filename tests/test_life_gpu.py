@@ -121,3 +121,23 @@ def test_life_few_ctas_many_tiles(cuda, oracle_mod, ctas):
     got = run2d(cuda, life_stencil(keep), a, b, 23,
                 sched=dict(time_steps=9, tile_w=0, tile_h=50, tile_d=0, ctas=ctas), dtype="u8")
     assert np.array_equal(got, oracle_mod.life(a, b, 23))
+
+
+@pytest.mark.parametrize("W,H", [(300, 1700), (333, 2100), (1000, 2500)])
+@pytest.mark.parametrize("iters", [2, 3, 25, 26, 51, 200])
+def test_life_host_run_overlapped(cuda, oracle_mod, W, H, iters):
+    """pskel_run2d_host on grids of 8+ tile rows: rows are copied in and packed
+    while the first passes run on the rows already there, and final rows are
+    unpacked and copied out while the last passes run on the others."""
+    keep = P._Keep()
+    a, b = grids(W, H, seed=W + iters)
+    got = P.run2d_host(life_stencil(keep), a, b.copy(), iters)
+    assert np.array_equal(got, oracle_mod.life(a, b, iters))
+
+
+@pytest.mark.parametrize("iters", [7, 60])
+def test_life_host_run_overlapped_ring2(cuda, oracle_mod, iters):
+    keep = P._Keep()
+    a, b = grids(517, 1900, seed=iters)
+    got = P.run2d_host(life_stencil(keep, rng=2), a, b.copy(), iters)
+    assert np.array_equal(got, oracle_mod.life(a, b, iters, rng=2))

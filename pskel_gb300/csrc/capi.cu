@@ -838,6 +838,16 @@ pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* out, int64
   return iterate_float2d(*st, in, out, width, height, pitch, iterations, R, ring, sched, c, s);
 }
 
+// Waits for a host call's copy streams on every return path, so that no copy
+// touches the caller's arrays after the call has returned.
+struct StreamDrain {
+  cudaStream_t a, b;
+  ~StreamDrain() {
+    cudaStreamSynchronize(a);
+    cudaStreamSynchronize(b);
+  }
+};
+
 // Events of one host call, destroyed when it returns.
 struct EventSet {
   std::vector<cudaEvent_t> ev;
@@ -932,6 +942,7 @@ static pskel_status run_life_host_wavefront(const uint8_t* in_host, uint8_t* out
   const int64_t pitch = static_cast<int64_t>(pitch_bytes);
   const int64_t resident = static_cast<int64_t>(life_bits_persistent_ctas_per_sm()) * c->sms;
   cudaStream_t s = c->stream, s_in = c->copy_in, s_out = c->copy_out;
+  StreamDrain drain{s_in, s_out};
   const int CT = (tiles_y + kLifeChunks - 1) / kLifeChunks;  // tile rows per chunk
   const int C = (tiles_y + CT - 1) / CT;
   EventSet ev;
@@ -1077,24 +1088,8 @@ pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void
   if (iterations >= 1 && ring > 0) {
     // The output array's ring is read by every second step and is part of the
     // result when the iteration count is odd; its interior is never read.
-    const uint8_t* oh = static_cast<const uint8_t*>(out_host);
-    uint8_t* od = static_cast<uint8_t*>(c->host_out.ptr);
-    const size_t r = static_cast<size_t>(std::min<int64_t>(ring, height));
-    e = cudaMemcpy2DAsync(od, pitch_bytes, oh, row, row, r, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && height > ring) {
-      const size_t top = static_cast<size_t>(height - r);
-      e = cudaMemcpy2DAsync(od + top * pitch_bytes, pitch_bytes, oh + top * row, row, row, r, cudaMemcpyHostToDevice, s);
-    }
-    if (e == cudaSuccess && height > 2 * ring) {
-      const size_t mid = static_cast<size_t>(height - 2 * ring);
-      const size_t cw = std::min<size_t>(static_cast<size_t>(ring), static_cast<size_t>(width)) * esz;
-      e = cudaMemcpy2DAsync(od + r * pitch_bytes, pitch_bytes, oh + r * row, row, cw, mid, cudaMemcpyHostToDevice, s);
-      if (e == cudaSuccess && width > ring) {
-        const size_t off = static_cast<size_t>(width - ring) * esz;
-        e = cudaMemcpy2DAsync(od + r * pitch_bytes + off, pitch_bytes, oh + r * row + off, row, cw, mid,
-                              cudaMemcpyHostToDevice, s);
-      }
-    }
+    e = copy_ring_h2d(static_cast<const uint8_t*>(out_host), static_cast<uint8_t*>(c->host_out.ptr), row,
+                      pitch_bytes, width, height, ring, esz, s);
     if (e != cudaSuccess) return cuda_fail(e, "copy output ring to device");
   }
   pskel_stencil dev = *st;
@@ -1207,6 +1202,7 @@ static pskel_status run3d_wavefront(const pskel_stencil& st, int64_t W, int64_t 
   EventSet ev;
   if ((e = ev.make(2 * static_cast<size_t>(C) + 1)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
   cudaStream_t s = c->stream, s_in = c->copy_in, s_out = c->copy_out;
+  StreamDrain drain{s_in, s_out};
   const uint8_t* hin = static_cast<const uint8_t*>(in_host);
   uint8_t* hout = static_cast<uint8_t*>(out_host);
   for (int64_t k = 0; k < C; ++k) {

@@ -63,6 +63,17 @@ __parallel__ void stencilKernel(Array3D<float> in, Array3D<float> out, Mask3D<fl
                                 size_t d) {
   stencilKernel(in, out, mask, HeatUser{0}, h, w, d);
 }
+// 2D functor reading a per-cell coefficient from an Args2D field (pinned host
+// memory mapped into the device): out = c + k * (((n + s) + (w + e)) - 4c)
+struct CoefArgs {
+  Args2D<float> coef;
+};
+__parallel__ void stencilKernel(Array2D<float> in, Array2D<float> out, Mask2D<float> mask, CoefArgs a, size_t h,
+                                size_t w) {
+  const float c = in(h, w);
+  const float sum = (mask.get(0, in, h, w) + mask.get(1, in, h, w)) + (mask.get(2, in, h, w) + mask.get(3, in, h, w));
+  out(h, w) = c + a.coef(static_cast<int>(w), static_cast<int>(h)) * (sum - 4.0f * c);
+}
 // 1D stencil: weighted sum over a 1D mask, halo value outside the array
 struct Smooth1D {
   int unused;
@@ -178,6 +189,24 @@ int main(int argc, char** argv) {
     } else {
       return 3;
     }
+    write_raw(fres, out.hostArray, W * H);
+  } else if (sc.rfind("coef", 0) == 0) {
+    // the coefficient field k(h, w) = 0.05 + 0.2 * ((h * 7 + w * 3) % 11) / 10
+    Array2D<float> in(W, H), out(W, H);
+    read_raw(fin, in.hostArray, W * H);
+    read_raw(fout, out.hostArray, W * H);
+    CoefArgs args{Args2D<float>(static_cast<int>(W), static_cast<int>(H))};
+    for (size_t h = 0; h < H; ++h)
+      for (size_t w = 0; w < W; ++w)
+        args.coef(static_cast<int>(w), static_cast<int>(h)) = 0.05f + 0.2f * static_cast<float>((h * 7 + w * 3) % 11) / 10.0f;
+    Mask2D<float> mask = jacobi_mask();
+    Stencil2D<Array2D<float>, Mask2D<float>, CoefArgs> st(in, out, mask, args);
+    if (sc == "coef_gpu")
+      st.runIterativeGPU(it, 0, 0);
+    else if (sc == "coef_cpu")
+      st.runIterativeCPU(it, 4);
+    else
+      return 3;
     write_raw(fres, out.hostArray, W * H);
   } else if (sc.rfind("stencil1d", 0) == 0) {
     // 1D: W cells; mask offsets -2, -1, 0, 1, 3 with halo value 0.5

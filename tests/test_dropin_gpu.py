@@ -200,3 +200,36 @@ def test_dropin_stencil1d(app, scenario, W, iters):
     got, _ = run_app(app, scenario, a, b, iters)
     want = smooth1d(a[0], iters)
     assert np.array_equal(got[0].view(np.uint32), want.view(np.uint32))
+
+
+def coef_run(a, b, iters):
+    """The app's Args2D functor restated: interior cells (ring 1) of the
+    destination get c + k * (((n + s) + (w + e)) - 4c) in fp32, rounded per
+    operation; each array keeps its ring; the result is in the output array
+    for odd counts, in the input array for even ones."""
+    H, W = a.shape
+    hh, ww = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    k = (np.float32(0.05) + np.float32(0.2) * ((hh * 7 + ww * 3) % 11).astype(np.float32) / np.float32(10.0))
+    k = k.astype(np.float32)
+    x, y = a.astype(np.float32).copy(), b.astype(np.float32).copy()
+    for it in range(iters):
+        src, dst = (x, y) if it % 2 == 0 else (y, x)
+        c = src[1:-1, 1:-1]
+        s1 = (src[:-2, 1:-1] + src[2:, 1:-1]).astype(np.float32)
+        s2 = (src[1:-1, :-2] + src[1:-1, 2:]).astype(np.float32)
+        sm = (s1 + s2).astype(np.float32)
+        d = (sm - (np.float32(4.0) * c).astype(np.float32)).astype(np.float32)
+        dst[1:-1, 1:-1] = (c + (k[1:-1, 1:-1] * d).astype(np.float32)).astype(np.float32)
+    return y if iters % 2 == 1 else x
+
+
+@pytest.mark.parametrize("scenario", ["coef_gpu", "coef_cpu"])
+@pytest.mark.parametrize("iters", [1, 4, 9])
+def test_dropin_args_field(app, scenario, iters):
+    """A user functor reading an Args2D field (mapped pinned host memory, the
+    reference's Args, PSkelArgs.hpp) on the GPU and on the host."""
+    rng = np.random.default_rng(iters)
+    a = rng.uniform(0, 1, (97, 131)).astype(np.float32)
+    b = rng.uniform(0, 1, (97, 131)).astype(np.float32)
+    got, _ = run_app(app, scenario, a, b, iters)
+    assert np.array_equal(got.view(np.uint32), coef_run(a, b, iters).view(np.uint32))

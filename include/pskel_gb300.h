@@ -27,7 +27,10 @@
  * points are synchronous and check it themselves.
  *
  * Not thread-safe, like the reference (its GA tuner uses a global evaluator,
- * PSkelStencil.hpp:1866-1881): one caller thread per process.
+ * PSkelStencil.hpp:1866-1881): one caller thread per process. The device
+ * entry points of one device share its scratch (Life bit planes, multi-pass
+ * counters, residual partials), so calls that overlap on the GPU (issued on
+ * two streams without an ordering between them) race.
  */
 #ifndef PSKEL_GB300_H
 #define PSKEL_GB300_H
@@ -111,6 +114,12 @@ PSKEL_API int32_t pskel_version(void);
 /* Message for the last failing call on this thread, "" if none. */
 PSKEL_API const char* pskel_last_error(void);
 
+/* Kernel launches (memsets not counted) issued by the calling thread's last
+ * pskel_iterate2d call; 0 after a call that failed before launching. No
+ * reference counterpart (a diagnostic: the reference launches one kernel per
+ * step, PSkelStencil.hpp:1078-1082). */
+PSKEL_API int64_t pskel_last_launches2d(void);
+
 /* Wait for `stream`, then report and clear the device error word. */
 PSKEL_API pskel_status pskel_sync(void* stream);
 
@@ -130,7 +139,12 @@ PSKEL_API int32_t pskel_plan_passes(int64_t iterations, int32_t time_steps, int3
  * `pitch` is the row pitch in elements (0 = width). The result ends in `out`
  * (odd iterations) or `in` (even), with its ring untouched; the other
  * buffer's contents afterwards are unspecified (the float paths ping-pong
- * through it, Life runs on internal bit planes and does not write it). */
+ * through it, Life runs on internal bit planes and does not write it).
+ * Reach-1 shapes and advection with several passes on grids of at most four
+ * waves of tiles run every pass in one persistent launch (tiles wait for
+ * their neighbourhood of the previous pass); the environment variable
+ * PSKEL_FAST2D_MULTIPASS=1 / 0 forces that launch on / off. Results are the
+ * same either way. */
 PSKEL_API pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* out, int64_t width, int64_t height,
                              int64_t pitch, int64_t iterations, const pskel_schedule* sched, void* stream);
 

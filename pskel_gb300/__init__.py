@@ -56,6 +56,8 @@ def _load():
     lib = C.CDLL(str(LIB_PATH))
     lib.pskel_version.restype = C.c_int32
     lib.pskel_last_error.restype = C.c_char_p
+    lib.pskel_last_launches2d.restype = C.c_int64
+    lib.pskel_last_launches2d.argtypes = []
     lib.pskel_sync.argtypes = [C.c_void_p]
     lib.pskel_iterate2d.argtypes = [C.POINTER(Stencil), C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                     C.c_int64, C.POINTER(Schedule), C.c_void_p]

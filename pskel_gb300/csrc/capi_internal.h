@@ -27,6 +27,7 @@ struct DeviceContext {
   DeviceBuffer res_acc;                            // 3D wavefront: squared sums per reported step
   DeviceBuffer life_bits;                          // Life: the two bit planes of a run
   DeviceBuffer life_sync;                          // Life: item counter and per-tile pass counts
+  DeviceBuffer fast2d_sync;                        // 2D multi-pass launches: item counter and per-tile pass counts
   DeviceBuffer tiles;                              // out-of-core runs: slab slots and both arrays' rings
 };
 

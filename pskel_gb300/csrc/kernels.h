@@ -108,11 +108,14 @@ cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* 
 // 1 = C,N,S,W,E; 2 = the 3x3 box row by row. Returns -1 for other masks.
 int fast2d_shape(const int* offsets, int n);
 // The default steps per pass of the reach-1 kernels (measured on GB300):
-// linear shapes 7 (4096^2 fp32: T=5/7 1.32/1.30 T cell updates/s, T=1 0.70);
+// linear shapes 7 (4096^2 fp32: T=5/7 1.32/1.30 T cell updates/s, T=1 0.70),
+// 11 on grids of at most 1M cells, which run every pass in one launch and
+// have fewer tiles than resident CTAs (1024^2 fp32: T=7/11/13 515/594/602
+// G cell updates/s; 1448^2: T=7/11 928/897);
 // advection fp32 5; advection bf16 1 (the HBM-bound streaming kernel) on
 // grids of 4M cells or more, else 7.
 inline int fast2d_default_steps(bool advect, int dtype, int64_t W, int64_t H) {
-  if (!advect) return 7;
+  if (!advect) return W * H <= (int64_t(1) << 20) ? 11 : 7;
   if (dtype != 2) return 5;
   return W * H >= (int64_t(1) << 22) ? 1 : 7;
 }
@@ -123,6 +126,19 @@ int fast2d_max_ctas_per_sm(bool advect, int dtype, int S);
 cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const CUtensorMap* md,
                         const CUtensorMap* mu, const CUtensorMap* mv, const Stencil2DParams& p, int ctas,
                         cudaStream_t s);
+
+// Every pass of a run in one persistent launch of the same tiles (for grids
+// of few tiles per pass): items (pass, tile) in order, each tile waiting
+// (bounded) for the tiles of the previous pass that its loaded tile overlaps.
+// Even passes read the buffer of map_in / p.src and write p.dst, odd passes
+// the reverse; pass i has 1 + 2 * (q + (i < r)) steps. `sync` (capacity
+// fast2d_multipass_sync_bytes, cleared here) holds the item counter and the
+// per-tile completion counts.
+size_t fast2d_multipass_smem_bytes(int dtype, int S);
+size_t fast2d_multipass_sync_bytes(int ntiles);
+cudaError_t fast2d_multipass(int opk, int dtype, int S, const CUtensorMap* map_in, const CUtensorMap* map_out,
+                             const Stencil2DParams& p, int npasses, int q, int r, void* sync, int ctas,
+                             cudaStream_t s);
 
 // One step of a reach-1 2D stencil of a known shape (opk 0..2) or advection
 // (opk 3), streaming (no temporal blocking), rows staged by TMA: persistent

@@ -127,6 +127,183 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   }
 }
 
+// One run of fast2d_multipass_kernel: the pass plan and the shared counters.
+struct Fast2DRun {
+  int npasses, q, r;              // pass i has 1 + 2 * (q + (i < r)) steps
+  unsigned long long* next_item;  // next (pass, tile) item to hand out
+  unsigned* done;                 // passes completed, one count per tile
+};
+
+constexpr unsigned kFastSpinLimit = 1u << 24;  // polls of a neighbour's completion count (each with a sleep)
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* q) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(q) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Every pass of a run in one persistent launch (grids of few tiles per pass,
+// where the end of each pass would leave SMs idle and every launch adds its
+// own latency). Work items (pass, tile) are handed out in order by an atomic
+// counter; before tile t of pass i is staged, thread 0 waits (bounded) until
+// each tile of pass i-1 whose core overlaps t's loaded tile has completed
+// (done[] counts the passes each tile has completed). Those tiles are also
+// the last readers of t's core in the buffer pass i writes. An awaited item
+// precedes the waiting one, so a running CTA holds it or has finished it.
+// Even passes read `in` (map_in) and write `out`, odd passes the reverse;
+// pass i has 1 + 2 * (q + (i < r)) steps (the odd-length plan).
+template <class TS, int OpK, int S>
+__global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
+    fast2d_multipass_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
+                            const __grid_constant__ Stencil2DParams p, const __grid_constant__ Fast2DRun run) {
+  constexpr int N = Vec<TS>::N;
+  constexpr int LW = 32 * N;
+  constexpr int LH = (kFastThreads / 32) * S + 2;
+  constexpr size_t kBuf = (static_cast<size_t>(LW) * LH * sizeof(TS) + 127) & ~size_t(127);
+  constexpr uint32_t kTileBytes = static_cast<uint32_t>(LW * LH * sizeof(TS));
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  if ((smem_u32(smem_raw) & 127u) != 0) {
+    if (threadIdx.x == 0) atomicOr(p.err, kDevErrAlign);
+    return;
+  }
+  TS* buf0 = reinterpret_cast<TS*>(smem_raw);
+  TS* buf1 = reinterpret_cast<TS*>(smem_raw + kBuf);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + 2 * kBuf);
+  __shared__ long long s_item;
+
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_barrier_init();
+    prefetch_tensormap(&map_in);
+    prefetch_tensormap(&map_out);
+  }
+  __syncthreads();
+  constexpr auto shp = shape_of<(OpK < 3 ? OpK : 0)>();
+  float wt[9];
+#pragma unroll
+  for (int n = 0; n < 9; ++n) wt[n] = (n < shp.n) ? p.wt[n] : 0.0f;
+
+  const int ntiles = p.tiles_x * p.tiles_y;
+  const long long nitems = static_cast<long long>(run.npasses) * ntiles;
+  const int dy = (p.HY + p.TH - 1) / p.TH;  // tile rows / columns whose cores the loaded tile overlaps
+  const int dx = (p.HX + p.TW - 1) / p.TW;
+  uint32_t phase_bits = 0;  // bit i: parity of the next completion of bars[i]
+  for (;;) {
+    if (tid == 0) s_item = static_cast<long long>(atomicAdd(run.next_item, 1ull));
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= nitems) break;
+    const int pass = static_cast<int>(item / ntiles);
+    const int tile = static_cast<int>(item - static_cast<long long>(pass) * ntiles);
+    const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
+    const int gy0 = ty * p.TH - p.HY;
+    const int gx0 = tx * p.TW - p.HX;
+    const int steps = 1 + 2 * (run.q + (pass < run.r ? 1 : 0));
+    const bool fwd = (pass & 1) == 0;
+    const bool ring_tile = (gy0 < p.ring) || (gy0 + LH > p.H - p.ring) || (gx0 < p.ring) || (gx0 + LW > p.W - p.ring);
+    const bool stage_dst = ring_tile && steps >= 2;
+    int ok = 1;
+    if (tid == 0) {
+      if (pass > 0) {
+        for (int yy = max(0, ty - dy); yy <= min(p.tiles_y - 1, ty + dy) && ok; ++yy) {
+          for (int xx = max(0, tx - dx); xx <= min(p.tiles_x - 1, tx + dx) && ok; ++xx) {
+            const unsigned* d = &run.done[yy * p.tiles_x + xx];
+            unsigned polls = 0;
+            while (ld_acquire_gpu(d) < static_cast<unsigned>(pass)) {
+              if (++polls >= kFastSpinLimit) {
+                atomicOr(p.err, kDevErrBarrier);
+                ok = 0;
+                break;
+              }
+              __nanosleep(32);
+            }
+          }
+        }
+      }
+      if (ok) {
+        // the previous pass wrote through the generic proxy, TMA reads through
+        // the async proxy; the buffers were last read by this CTA's threads
+        fence_proxy_async_global();
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bars[0], kTileBytes);
+        tma_load_2d(buf0, fwd ? &map_in : &map_out, gx0, gy0, &bars[0]);
+        if (stage_dst) {
+          mbar_arrive_expect_tx(&bars[1], kTileBytes);
+          tma_load_2d(buf1, fwd ? &map_out : &map_in, gx0, gy0, &bars[1]);
+        }
+        ok = mbar_wait_bounded(&bars[0], phase_bits & 1u, p.err) ? 1 : 0;
+        if (ok && stage_dst) ok = mbar_wait_bounded(&bars[1], (phase_bits >> 1) & 1u, p.err) ? 1 : 0;
+      }
+    }
+    if (!__syncthreads_and(ok)) break;
+    phase_bits ^= 1u;
+    if (stage_dst) phase_bits ^= 2u;
+
+    TileGeom g;
+    g.W = p.W;
+    g.H = p.H;
+    g.ring = p.ring;
+    g.steps = steps;
+    g.TW = p.TW;
+    g.TH = p.TH;
+    g.HX = p.HX;
+    g.HY = p.HY;
+    g.pitch = p.pitch;
+    g.K = p.K;
+    g.dt = p.dt;
+    g.inv_dx = p.inv_dx;
+    g.u = p.u;
+    g.v = p.v;
+    TS* dst = static_cast<TS*>(fwd ? p.dst : const_cast<void*>(p.src));
+    fast2d_run_tile<TS, OpK, S>(buf0, buf1, dst, g, gy0, gx0, ring_tile, wt);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+      fence_proxy_async_global();
+      atomicAdd(&run.done[tile], 1u);
+    }
+  }
+}
+
+template <class TS, int OpK, int S>
+cudaError_t launch_multipass(const CUtensorMap* mi, const CUtensorMap* mo, const Stencil2DParams& p,
+                             const Fast2DRun& run, int ctas, cudaStream_t s) {
+  const size_t smem = fast2d_multipass_smem_bytes(sizeof(TS) == 2 ? 2 : 1, S);
+  auto kern = fast2d_multipass_kernel<TS, OpK, S>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  // every CTA resident (items are taken only by running CTAs, so this is for
+  // speed, not for progress)
+  static int resident = 0;
+  if (resident == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastThreads, smem);
+    resident = (per_sm > 0 ? per_sm : 1) * sms;
+  }
+  if (ctas > resident) ctas = resident;
+  kern<<<ctas, kFastThreads, smem, s>>>(*mi, *mo, p, run);
+  return cudaGetLastError();
+}
+
+template <class TS, int S>
+cudaError_t dispatch_multipass(int opk, const CUtensorMap* mi, const CUtensorMap* mo, const Stencil2DParams& p,
+                               const Fast2DRun& run, int ctas, cudaStream_t s) {
+  switch (opk) {
+    case 0: return launch_multipass<TS, 0, S>(mi, mo, p, run, ctas, s);
+    case 1: return launch_multipass<TS, 1, S>(mi, mo, p, run, ctas, s);
+    case 2: return launch_multipass<TS, 2, S>(mi, mo, p, run, ctas, s);
+    default: return launch_multipass<TS, 3, S>(mi, mo, p, run, ctas, s);
+  }
+}
+
 template <class TS, int OpK, int S>
 cudaError_t launch_fast(const CUtensorMap* ms, const CUtensorMap* md, const CUtensorMap* mu, const CUtensorMap* mv,
                         const Stencil2DParams& p, int ctas, cudaStream_t s) {
@@ -196,6 +373,33 @@ int fast2d_max_ctas_per_sm(bool advect, int dtype, int S) {
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   const int by_smem = static_cast<int>(per_sm / (smem + 1024));
   return by_smem < 8 ? by_smem : 8;
+}
+
+size_t fast2d_multipass_smem_bytes(int dtype, int S) {
+  const size_t esz = (dtype == 2) ? 2 : 4;
+  const size_t buf = (static_cast<size_t>(128) * (16 * S + 2) * esz + 127) & ~size_t(127);
+  return 128 + 2 * buf + 16;
+}
+
+size_t fast2d_multipass_sync_bytes(int ntiles) { return 16 + 4 * static_cast<size_t>(ntiles); }
+
+cudaError_t fast2d_multipass(int opk, int dtype, int S, const CUtensorMap* map_in, const CUtensorMap* map_out,
+                             const Stencil2DParams& p, int npasses, int q, int r, void* sync, int ctas,
+                             cudaStream_t s) {
+  const int ntiles = p.tiles_x * p.tiles_y;
+  cudaError_t e = cudaMemsetAsync(sync, 0, fast2d_multipass_sync_bytes(ntiles), s);
+  if (e != cudaSuccess) return e;
+  Fast2DRun run;
+  run.npasses = npasses;
+  run.q = q;
+  run.r = r;
+  run.next_item = static_cast<unsigned long long*>(sync);
+  run.done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
+  if (dtype == 2)
+    return S == 8 ? dispatch_multipass<__nv_bfloat16, 8>(opk, map_in, map_out, p, run, ctas, s)
+                  : dispatch_multipass<__nv_bfloat16, 4>(opk, map_in, map_out, p, run, ctas, s);
+  return S == 8 ? dispatch_multipass<float, 8>(opk, map_in, map_out, p, run, ctas, s)
+                : dispatch_multipass<float, 4>(opk, map_in, map_out, p, run, ctas, s);
 }
 
 cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const CUtensorMap* md,

@@ -270,3 +270,36 @@ def test_advection_streaming(cuda, oracle_mod, dtype, W, H, th):
     got = _advect_gpu(cuda, dtype, a, b, u, v, 9, sch=sched(1, 0, th))
     want = oracle_mod.advect(a, b, u, v, 9, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype=dtype)
     assert np.array_equal(bits(got), bits(want))
+
+
+_MP_SHAPES = {
+    "jacobi4": (S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS),
+    "cross5": (CROSS5_OFFSETS, CROSS5_WEIGHTS),
+    "box9": (BOX9_OFFSETS, BOX9_WEIGHTS),
+}
+
+
+@pytest.mark.parametrize("mode", ["1", "0"])
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("op", ["jacobi4", "cross5", "box9", "advect"])
+@pytest.mark.parametrize("W,H,iters,T,ctas", [(517, 389, 19, 7, 0), (1024, 1024, 100, 0, 0), (130, 70, 40, 15, 0),
+                                               (33, 900, 12, 3, 0), (300, 260, 21, 5, 3), (129, 131, 10, 3, 1)])
+def test_multipass_launch(cuda, oracle_mod, monkeypatch, mode, dtype, op, W, H, iters, T, ctas):
+    # every pass in one persistent launch (tiles wait for their neighbourhood
+    # of the previous pass) and one launch per pass give the oracle's bits;
+    # ctas 1 and 3 make a few CTAs walk many (pass, tile) items in order
+    monkeypatch.setenv("PSKEL_FAST2D_MULTIPASS", mode)
+    if op == "advect":
+        a, b, u, v = _advect_inputs(W, H, W + iters, dtype)
+        got = _advect_gpu(cuda, dtype, a, b, u, v, iters, sch=sched(T, 0, 0, ctas))
+        want = oracle_mod.advect(a, b, u, v, iters, S.ADVECT_K, S.ADVECT_DT, S.ADVECT_INV_DX, dtype=dtype)
+    else:
+        offsets, weights = _MP_SHAPES[op]
+        if dtype == "bf16":
+            weights = [float(S.bf16_to_f32(S.f32_to_bf16(np.array([w], np.float32)))[0]) for w in weights]
+        keep = P._Keep()
+        st = P.make_stencil(P.OP_LINEAR, dtype, offsets, weights, keep=keep)
+        a, b = jac_grids(W, H, W + iters, dtype)
+        got = run2d(cuda, st, a, b, iters, sched=sched(T, 0, 0, ctas), dtype=dtype)
+        want = oracle_mod.lin2d(a, b, offsets, weights, iters, dtype=dtype)
+    assert np.array_equal(bits(got), bits(want))

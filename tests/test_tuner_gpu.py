@@ -134,8 +134,9 @@ def _training_set(torch, st, shapes, reps=3):
 
 def test_trained_model_beats_default_and_ga(cuda):
     """Trained on measured timings of one set of grids, the model's picks on
-    held-out grids run faster in total than the library's default schedule and
-    than the GA's pick, and stay close to the exhaustive tuner's."""
+    held-out grids run faster in total than the library's default schedule, at
+    least as fast as the GA's pick (within timing noise), and stay close to the
+    exhaustive tuner's."""
     torch = cuda
     keep = P._Keep()
     st = P.make_stencil(P.OP_LINEAR, "f32", S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, keep=keep)
@@ -162,9 +163,14 @@ def test_trained_model_beats_default_and_ga(cuda):
             tot["ga"] += t[2]
             tot["best"] += ms.min()
         print({k: round(v, 4) for k, v in tot.items()})
-        # measured on GB300 over several runs: model/best 1.13-1.22, model/GA
-        # 0.83-0.90, model/default 0.67-0.73 (timing noise moves each run)
-        assert tot["model"] < tot["ga"]
+        # measured on GB300 over several runs with one launch per pass:
+        # model/best 1.13-1.22, model/GA 0.83-0.90, model/default 0.67-0.73.
+        # Grids of this size now run every pass in one persistent launch, where
+        # the GA's long passes (T = 15, tall tiles) are close to the best too:
+        # model/best 1.007, model/GA 0.990, model/default 0.918. The bound
+        # allows timing noise; the learned batched launch against the GA-tuned
+        # per-grid launches (4.6x in the batch bench) is the larger gain.
+        assert tot["model"] <= 1.02 * tot["ga"]
         assert tot["model"] <= 1.02 * tot["default"]
         assert tot["model"] <= 1.35 * tot["best"]
         # registered, it is what pskel_auto_schedule2d returns

@@ -65,6 +65,9 @@ pskel_status get_context(DeviceContext** out) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(error word)");
   e = cudaMemset(c->err, 0, 64);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error word)");
+  e = cudaHostAlloc(reinterpret_cast<void**>(&c->err_host), 64, cudaHostAllocDefault);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc(error word copy)");
+  *c->err_host = 0;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking);
@@ -86,11 +89,13 @@ pskel_status ensure_buffer(DeviceBuffer& b, size_t bytes) {
 }
 
 pskel_status device_sync_check(DeviceContext* c, cudaStream_t s) {
-  cudaError_t e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
-  unsigned word = 0;
-  e = cudaMemcpy(&word, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  // the error word follows the stream's work in a copy to pinned host memory,
+  // so one synchronisation covers both
+  cudaError_t e = cudaMemcpyAsync(c->err_host, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  const cudaError_t es = cudaStreamSynchronize(s);
+  if (es != cudaSuccess) return cuda_fail(es, "kernel execution");
   if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
+  const unsigned word = *static_cast<volatile unsigned*>(c->err_host);
   if (word) {
     cudaMemset(c->err, 0, sizeof(unsigned));
     std::string msg = "device error:";
@@ -1121,27 +1126,38 @@ pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void
   const int64_t pitch = static_cast<int64_t>(pitch_bytes / esz);
   if (pskel_status s = ensure_buffer(c->host_in, bytes)) return s;
   if (pskel_status s = ensure_buffer(c->host_out, bytes)) return s;
-  cudaStream_t s = c->stream;
-  cudaError_t e = cudaMemcpy2DAsync(c->host_in.ptr, pitch_bytes, in_host, row, row, height, cudaMemcpyHostToDevice, s);
+  if (st->op == PSKEL_OP_ADVECT) {
+    if (pskel_status q = ensure_buffer(c->host_u, bytes)) return q;
+    if (pskel_status q = ensure_buffer(c->host_v, bytes)) return q;
+  }
+  // The input goes over on the compute stream; the output array's ring (many
+  // short rows: its columns) and the winds go over on the copy stream at the
+  // same time, and the compute stream waits for them.
+  cudaStream_t s = c->stream, s_in = c->copy_in;
+  StreamDrain drain{s_in, s_in};
+  EventSet ev;
+  cudaError_t e = ev.make(1);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+  e = cudaMemcpy2DAsync(c->host_in.ptr, pitch_bytes, in_host, row, row, height, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "copy input to device");
   if (iterations >= 1 && ring > 0) {
     // The output array's ring is read by every second step and is part of the
     // result when the iteration count is odd; its interior is never read.
     e = copy_ring_h2d(static_cast<const uint8_t*>(out_host), static_cast<uint8_t*>(c->host_out.ptr), row,
-                      pitch_bytes, width, height, ring, esz, s);
+                      pitch_bytes, width, height, ring, esz, s_in);
     if (e != cudaSuccess) return cuda_fail(e, "copy output ring to device");
   }
   pskel_stencil dev = *st;
   if (st->op == PSKEL_OP_ADVECT) {
-    if (pskel_status q = ensure_buffer(c->host_u, bytes)) return q;
-    if (pskel_status q = ensure_buffer(c->host_v, bytes)) return q;
-    e = cudaMemcpy2DAsync(c->host_u.ptr, pitch_bytes, st->wind_u, row, row, height, cudaMemcpyHostToDevice, s);
+    e = cudaMemcpy2DAsync(c->host_u.ptr, pitch_bytes, st->wind_u, row, row, height, cudaMemcpyHostToDevice, s_in);
     if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(c->host_v.ptr, pitch_bytes, st->wind_v, row, row, height, cudaMemcpyHostToDevice, s);
+      e = cudaMemcpy2DAsync(c->host_v.ptr, pitch_bytes, st->wind_v, row, row, height, cudaMemcpyHostToDevice, s_in);
     if (e != cudaSuccess) return cuda_fail(e, "copy wind fields to device");
     dev.wind_u = c->host_u.ptr;
     dev.wind_v = c->host_v.ptr;
   }
+  if ((e = cudaEventRecord(ev.ev[0], s_in)) != cudaSuccess || (e = cudaStreamWaitEvent(s, ev.ev[0], 0)) != cudaSuccess)
+    return cuda_fail(e, "ordering the copies before the run");
   if (pskel_status q = pskel_iterate2d(&dev, c->host_in.ptr, c->host_out.ptr, width, height, pitch, iterations, sched, s))
     return q;
   const void* result = (iterations % 2 == 1) ? c->host_out.ptr : c->host_in.ptr;

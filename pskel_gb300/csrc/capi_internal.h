@@ -19,6 +19,7 @@ struct DeviceContext {
   int sms = 0;
   int smem_optin = 0;
   unsigned* err = nullptr;        // device error word (kernels atomicOr into it)
+  unsigned* err_host = nullptr;   // pinned host copy of it, read after a stream's copy lands
   cudaStream_t stream = nullptr;  // stream of the *_host entry points
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // their overlapped copies
   DeviceBuffer host_in, host_out, host_u, host_v;  // staging for *_host

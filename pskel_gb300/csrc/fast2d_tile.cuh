@@ -131,12 +131,23 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
   const int lane = tid & 31, warp = tid >> 5;
   const int x0 = lane * N;
   const int yb = 1 + warp * S;
+  constexpr int LH = (kFastThreads / 32) * S + 2;
   const TS* wu = static_cast<const TS*>(g.u);
   const TS* wv = static_cast<const TS*>(g.v);
   const int gxv = gx0 + x0;
   for (int s = 1; s <= g.steps; ++s) {
     const TS* in = ((s & 1) ? sbuf : pbuf);
     TS* out = ((s & 1) ? pbuf : sbuf);
+    // After step s only rows [s, LH - s) are exact (the tile edges feed
+    // garbage in one row per step) and only they are read by step s + 1 and
+    // by the write-back (core rows [HY, LH - HY), HY >= steps). Rows outside
+    // are not computed: whatever the buffer holds there is never used, and a
+    // ring cell there keeps the buffer's value as a computed one would. The
+    // test is uniform per warp; a warp with no such row skips the step.
+    if (yb + S <= s || yb >= LH - s) {
+      __syncthreads();
+      continue;
+    }
     // window: rows yb-1 .. yb+S, each [left, v0..v3, right]; the left and
     // right neighbours come from the adjacent lanes (one warp spans a row)
     float win[S + 2][N + 2];
@@ -149,6 +160,7 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
 #pragma unroll
     for (int k = 1; k <= S; ++k) {
       const int y = yb - 1 + k;
+      if (y < s || y >= LH - s) continue;
       float res[N];
       if constexpr (!kAdvect) {
 #pragma unroll

@@ -10,9 +10,9 @@
 // bits fp32, 64 bits bf16) plus its two edge neighbours, keeping a
 // (S + 2)-row window in registers. The tile is 128 cells wide and
 // 16 * S + 2 rows high (16 warps of S rows each);
-// every step computes the whole tile minus its outer row, and garbage from the
-// tile edges advances one cell per step into the halo, which the core never
-// reaches in T <= halo steps.
+// garbage from the tile edges advances one cell per step into the halo, which
+// the core never reaches in T <= halo steps; step s computes the full width
+// and only the rows [s, LH - s) that are still exact.
 //
 // Arithmetic is the oracle's: products and sums in mask order with
 // __fmul_rn/__fadd_rn (no contraction), bf16 results rounded every step.

@@ -885,10 +885,10 @@ pskel_status pskel_iterate2d(const pskel_stencil* st, void* in, void* out, int64
 // Waits for a host call's copy streams on every return path, so that no copy
 // touches the caller's arrays after the call has returned.
 struct StreamDrain {
-  cudaStream_t a, b;
+  cudaStream_t a, b;  // b may be null (one stream)
   ~StreamDrain() {
     cudaStreamSynchronize(a);
-    cudaStreamSynchronize(b);
+    if (b) cudaStreamSynchronize(b);
   }
 };
 
@@ -1134,7 +1134,7 @@ pskel_status pskel_run2d_host(const pskel_stencil* st, const void* in_host, void
   // short rows: its columns) and the winds go over on the copy stream at the
   // same time, and the compute stream waits for them.
   cudaStream_t s = c->stream, s_in = c->copy_in;
-  StreamDrain drain{s_in, s_in};
+  StreamDrain drain{s_in, nullptr};
   EventSet ev;
   cudaError_t e = ev.make(1);
   if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");

@@ -85,6 +85,7 @@ def test_invalid_arguments_rejected_without_gpu(case):
     rc = _iterate(st, a, b, W, H, pitch, iters)
     assert rc == expect, P.lib.pskel_last_error().decode()
     assert P.lib.pskel_last_error().decode() != ""
+    assert P.lib.pskel_last_launches2d() == 0  # rejected before any launch
 
 
 def test_pass_plan_parity():

@@ -303,3 +303,6 @@ def test_multipass_launch(cuda, oracle_mod, monkeypatch, mode, dtype, op, W, H, 
         got = run2d(cuda, st, a, b, iters, sched=sched(T, 0, 0, ctas), dtype=dtype)
         want = oracle_mod.lin2d(a, b, offsets, weights, iters, dtype=dtype)
     assert np.array_equal(bits(got), bits(want))
+    # every case has several passes: one launch in all, or one per pass
+    launches = P.lib.pskel_last_launches2d()
+    assert launches == 1 if mode == "1" else launches > 1

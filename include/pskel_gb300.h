@@ -140,7 +140,7 @@ PSKEL_API int32_t pskel_plan_passes(int64_t iterations, int32_t time_steps, int3
  * (odd iterations) or `in` (even), with its ring untouched; the other
  * buffer's contents afterwards are unspecified (the float paths ping-pong
  * through it, Life runs on internal bit planes and does not write it).
- * Reach-1 shapes and advection with several passes on grids of at most four
+ * Reach-1 shapes and advection with several passes on grids of at most three
  * waves of tiles run every pass in one persistent launch (tiles wait for
  * their neighbourhood of the previous pass); the environment variable
  * PSKEL_FAST2D_MULTIPASS=1 / 0 forces that launch on / off. Results are the

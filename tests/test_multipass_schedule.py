@@ -7,8 +7,9 @@ item waits until every tile of pass i-1 whose core overlaps its loaded tile
 This test restates that schedule with loads and stores as separate events,
 runs it under many random interleavings of the CTAs, and checks the result
 against the step-by-step ping-pong of the reference (ring cells never
-written, PSkelStencil.hpp:2197-2257). A wait set one tile too small is caught
-by the same check.
+written, PSkelStencil.hpp:2197-2257). Each tile computes at step s only the
+rows [s, LH - s) that are still exact, as the tile routine does. A wait set
+one tile too small, or one row fewer computed, is caught by the same check.
 """
 from __future__ import annotations
 
@@ -42,8 +43,11 @@ def reference(a, b, passes, ring):
     return y if sum(passes) % 2 else x
 
 
-def run_tile(bufs, i, t, steps, geo, ring):
-    """Load phase of item (i, t): stage src (and dst for its ring) tiles."""
+def run_tile(bufs, i, t, steps, geo, ring, exact_margin=0):
+    """Load phase of item (i, t): stage src (and dst for its ring) tiles,
+    then the steps. Step s computes only the tile rows [s, LH - s), the rows
+    still exact (exact_margin > 0 drops that many more on each side: a
+    planted mistake); other rows keep whatever the buffer held."""
     H, W, TW, TH, HX, HY, tx_n = geo
     src, dst = (0, 1) if i % 2 == 0 else (1, 0)
     ty, tx = divmod(t, tx_n)
@@ -61,12 +65,14 @@ def run_tile(bufs, i, t, steps, geo, ring):
     gx = np.arange(gx0, gx0 + LW)[None, :]
     interior = (gy >= ring) & (gy < H - ring) & (gx >= ring) & (gx < W - ring)
     cur, other = s_tile, d_tile
-    for _ in range(steps):
+    rows = np.arange(LH)[:, None]
+    for s in range(1, steps + 1):
         nxt = other.copy()
         acc = np.zeros((LH - 2, LW - 2))
         for (dh, dw), w in zip(OFFS, WTS):
             acc = acc + w * cur[1 + dh:LH - 1 + dh, 1 + dw:LW - 1 + dw]
-        inner = interior[1:-1, 1:-1]
+        live = (rows >= s + exact_margin) & (rows < LH - s - exact_margin)
+        inner = (interior & live)[1:-1, 1:-1]
         nxt[1:-1, 1:-1][inner] = acc[inner]
         cur, other = nxt, cur
     # the store phase writes the core's interior cells into dst
@@ -84,7 +90,7 @@ def store(bufs, dst, gy0, gx0, core, mask, geo):
     region[m] = c[m]
 
 
-def simulate(a, b, passes, ring, TW, TH, T, ctas, rng, dy=None, dx=None):
+def simulate(a, b, passes, ring, TW, TH, T, ctas, rng, dy=None, dx=None, exact_margin=0):
     H, W = a.shape
     HY, HX = T, T
     tx_n, ty_n = math.ceil(W / TW), math.ceil(H / TH)
@@ -112,7 +118,7 @@ def simulate(a, b, passes, ring, TW, TH, T, ctas, rng, dy=None, dx=None):
                                   for yy in range(max(0, ty - dy), min(ty_n, ty + dy + 1))
                                   for xx in range(max(0, tx - dx), min(tx_n, tx + dx + 1)))
             if ready:
-                c[0], c[2] = "stored", run_tile(bufs, i, t, passes[i], geo, ring)
+                c[0], c[2] = "stored", run_tile(bufs, i, t, passes[i], geo, ring, exact_margin)
         elif phase == "stored":
             store(bufs, *staged, geo)
             done[t] += 1
@@ -156,3 +162,15 @@ def test_a_smaller_wait_set_is_caught():
         got = simulate(a, b, passes, 1, TW, TH, T, 100, np.random.default_rng(trial), dy=0)
         wrong += not np.array_equal(got, want)
     assert wrong > 0
+
+
+def test_computing_one_row_fewer_is_caught():
+    # the tile routine computes rows [s, LH - s) at step s; one row fewer on
+    # each side leaves stale values inside the core after a full-length pass
+    H, W, TW, TH, T, passes = 40, 33, 6, 5, 5, [5, 3, 3, 1, 1]
+    rng = np.random.default_rng(4)
+    a = rng.random((H, W))
+    b = rng.random((H, W))
+    want = reference(a, b, passes, 1)
+    got = simulate(a, b, passes, 1, TW, TH, T, 7, np.random.default_rng(0), exact_margin=1)
+    assert not np.array_equal(got, want)

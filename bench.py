@@ -2,8 +2,8 @@
 
 Default workload (the headline configuration): Game of Life, Moore mask,
 uint8 cells Bernoulli(0.3) from a seed, 8192 x 8192 grid, 1000 generations
-per step, temporal blocking of 25 generations per pass. A "step" is one full
-1000-generation run over the grid.
+per step, temporally blocked passes. A "step" is one full 1000-generation run
+over the grid.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload life|jacobi|jacobi_bf16|advect|advect_bf16|heat3d|heat3d_bf16|batch|batch_bf16]
@@ -12,8 +12,12 @@ Prints ONE JSON line. ``value`` is GCells/s (cell updates per second) with the
 grid resident in HBM; ``e2e`` is the same metric through the host entry point
 (pskel_run2d_host: host->device copy from pinned memory, the run, the copy
 back). ``--impl reference`` times the reference's own OpenMP runIterativeCPU
-(oracle/_ref/pskel_ref, built from the reference headers) on the host cores on
-a bounded sample of the same workload.
+(oracle/_ref/pskel_ref, built from the reference headers) on the host cores,
+every timed step running the whole workload.
+
+A single-GPU run of the headline workload also measures every other workload
+(at most 5 timed steps each, a smaller CPU sample) and reports them under
+``others``; ``--no-others`` skips that.
 
 Under torchrun (N > 1) every rank runs an independent replica of the
 workload on its own GPU (the path has no cross-grid exchange); the timing is
@@ -61,6 +65,17 @@ WORKLOADS = {
                             "graph, MLP-picked steps per pass",
                        grids=256, train_grids=64, dtype="bf16", batch=True, W=1024, H=1024, iters=100),
 }
+
+
+L2_NOTE = ("every timed step starts from freshly written inputs; the GPU arm also writes 512 MB (more than the "
+           "L2) between timed steps")
+
+
+def workload_config(wl, world):
+    """The workload as both arms run it (the GPU arm's schedule is reported beside it)."""
+    grid = [wl["H"], wl["W"]] + ([wl["D"]] if "D" in wl else [])
+    return {"workload": wl["desc"], "grid": grid, "iterations_per_step": wl["iters"], "l2": L2_NOTE,
+            "parallelism": "one replica per rank" if world > 1 else "single replica"}
 
 
 def load_peaks():
@@ -386,22 +401,21 @@ def run_ours(args, wl, world, rank, local):
     pass_bytes = b_alg * W * H * D * (passes / dom)
     if wl["name"] == "life":
         pass_bytes = 3 * W * H  # HBM: pack reads both byte grids, unpack writes one; the bit planes stay in L2
-    traffic = load_traffic(wl["name"])
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_dev / args.steps * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": wl["desc"], "grid": [H, W, D] if is3d else [H, W], "iterations_per_step": iters,
-                   "time_steps_per_pass": sch.time_steps, "passes": passes, "l2": "flushed between timed steps (512 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(wl, world),
+        "schedule": {"time_steps_per_pass": sch.time_steps, "passes": passes},
         "e2e": {"value": round(e2e_value, 3), "unit": "GCells/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "matches_device_run": same},
         "plain": plain if plain is not None else {"note": "the tuned schedule is one step per pass"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "traffic": traffic,
+                     "frac": round(achieved / peak, 3), "traffic": None,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
+                     "algorithmic_bytes_per_launch": b_alg * W * H * D * (iters / dom),
                      "per_launch_ms": round(per_launch_ms, 5),
                      "pass_compulsory_frac": round(pass_bytes / (per_launch_ms / 1e3) / 1e9 / peak, 3),
                      "note": "achieved = B_alg per cell update x cell updates per launch / launch time; "
@@ -614,9 +628,8 @@ def run_batch(args, wl, world, rank, local):
         "metric": METRIC, "value": round(value, 3), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_learned / args.steps * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": wl["desc"], "grids": len(shapes), "cell_updates_per_step": cells,
-                   "l2": "flushed between timed steps (512 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": {"workload": wl["desc"], "grids": len(shapes), "cell_updates_per_step": cells, "l2": L2_NOTE,
+                   "parallelism": "one replica per rank" if world > 1 else "single replica"},
         "tuning": {"learned_batch": round(value, 3), "exhaustive_batch": round(v_exh, 3),
                    "default_batch": round(v_def, 3), "ga_plain_launches": round(v_ga, 3),
                    "uniform_batch": {str(t): round(v, 3) for t, v in uniform.items()},
@@ -632,9 +645,10 @@ def run_batch(args, wl, world, rank, local):
                 "h2d_bytes_per_step": pool_bytes, "d2h_bytes_per_step": pool_bytes},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "traffic": load_traffic(wl["name"]),
+                     "frac": round(achieved / peak, 3), "traffic": None,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
+                     "algorithmic_bytes_per_launch": b_alg * cells,
                      "per_launch_ms": round(per_launch * 1e3, 4), "passes_per_launch": passes,
                      "pass_compulsory_frac": round(pass_bytes / per_launch / 1e9 / peak, 3),
                      "note": "one persistent launch runs every pass of every grid; achieved = B_alg x cell "
@@ -657,14 +671,60 @@ def plan_any(iters, T):
     return p
 
 
-def load_traffic(name):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "traffic.json"
+def load_counters(name):
+    """ncu counters of the workload's dominant kernel, per launch, from the
+    committed summary (profiles/counters.json): DRAM bytes, warp instructions
+    issued and ALU-pipe warp instructions, with the summary they come from."""
+    p = ROOT / "profiles" / "counters.json"
     if p.exists():
-        d = json.loads(p.read_text())
-        if name in d:
-            return d[name]
-    return None
+        return json.loads(p.read_text()).get(name, {})
+    return {}
+
+
+ISSUE_PER_SM_CLK = 4  # warp instructions an SM issues per clock (four schedulers)
+ALU_PER_SM_CLK = 2    # ALU-pipe warp instructions an SM completes per clock (16 lanes per scheduler)
+
+
+def finish_roofline(line, name, clocks, sms):
+    """Picks the roof of the dominant kernel. Its HBM figure (algorithmic bytes
+    per launch / launch time / measured copy bandwidth) is the roofline when
+    the kernel moves about its algorithmic bytes. A kernel whose DRAM traffic
+    (ncu) is far below them -- temporal blocking keeps the grid on chip -- is
+    bound by instruction issue instead: achieved = warp instructions per
+    launch (ncu) / launch time, peak = SMs x 4 schedulers x SM clock sampled
+    during the timed region. The HBM figure is kept beside it."""
+    rf = line["roofline"]
+    c = load_counters(name)
+    rf["traffic"] = c.get("dram_bytes")
+    alg = rf.pop("algorithmic_bytes_per_launch")
+    if not (c.get("dram_bytes") is not None and c.get("warp_instructions") and c["dram_bytes"] < 0.5 * alg):
+        rf["counters_from"] = c.get("profile")
+        return
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not mhz:
+        return
+    t = rf["per_launch_ms"] / 1e3
+    hbm = {k: rf[k] for k in ("achieved", "peak", "unit", "frac", "peak_source")}
+    issue = c["warp_instructions"] / t / 1e9
+    peak = sms * ISSUE_PER_SM_CLK * mhz * 1e6 / 1e9
+    line["roofline"] = {
+        "bound": "issue", "achieved": round(issue, 1), "peak": round(peak, 1), "unit": "G warp instructions/s",
+        "frac": round(issue / peak, 3), "traffic": c["dram_bytes"],
+        "peak_source": f"{sms} SMs x {ISSUE_PER_SM_CLK} schedulers x {mhz:.0f} MHz (median SM clock sampled "
+                       "during the timed region)",
+        "per_launch_ms": rf["per_launch_ms"],
+        "warp_instructions_per_launch": c["warp_instructions"], "counters_from": c.get("profile"),
+        "hbm_algorithmic": dict(hbm, note="algorithmic bytes per launch / launch time; above 1 because the grid "
+                                          "stays on chip between steps (bytes_avoided_factor = frac)"),
+        "bytes_avoided_factor": hbm["frac"],
+        "dram_frac_of_algorithmic": round(c["dram_bytes"] / alg, 6),
+    }
+    if c.get("alu_warp_instructions"):
+        line["roofline"]["alu_pipe_frac"] = round(
+            c["alu_warp_instructions"] / t / (sms * ALU_PER_SM_CLK * mhz * 1e6), 3)
+    for k in ("pass_compulsory_frac", "passes_per_launch"):
+        if k in rf:
+            line["roofline"][k] = rf[k]
 
 
 # ------------------------------------------------------- CPU baselines
@@ -732,12 +792,14 @@ def run_reference_arm(args, wl, world, rank):
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
-    # per step: the whole workload when it is small, else a bounded sample of
-    # its iterations, so that the whole run stays within a few minutes
-    its = min(wl["iters"], sample_iters(wl, updates=5e9))
+    # every timed step runs the whole workload (Life 8192^2 x 1000: about
+    # 30 s on 16 Grace cores), so the arm's config is the GPU arm's; the
+    # untimed warm-up steps run a tenth of the iterations (they only page in
+    # the binary and the inputs)
+    its = wl["iters"]
     vals, kind, walls = [], None, []
     for _ in range(args.warmup):
-        cpu_sample(wl, threads, max(1, its // 4))
+        cpu_sample(wl, threads, max(1, its // 10))
     for _ in range(args.steps):
         v, kind, w = cpu_sample(wl, threads, its)
         vals.append(v)
@@ -753,11 +815,58 @@ def run_reference_arm(args, wl, world, rank):
     return {"metric": METRIC, "value": round(value, 4), "unit": "GCells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(sum(walls) / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": wl["desc"], "grid": [wl["H"], wl["W"]], "iterations_per_step": its},
+            "config": workload_config(wl, world),
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 4), "unit": "GCells/s", "cores": threads, "kind": kind,
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "GCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+OTHERS = ["jacobi", "jacobi_bf16", "advect", "advect_bf16", "heat3d", "heat3d_bf16", "batch", "batch_bf16"]
+
+
+def cpu_baseline(wl, updates):
+    """The reference's runIterativeCPU on the host cores: runs of at most the
+    workload's iterations (the whole workload when it is small, repeated up to
+    10 times), about `updates` cell updates in all."""
+    total = sample_iters(wl, updates)
+    its = min(wl["iters"], total)
+    reps = min(10, max(1, total // its))
+    shape = "x".join(str(v) for v in ([wl["H"], wl["W"]] + ([wl["D"]] if "D" in wl else [])))
+    kind, wall = None, 0.0
+    for _ in range(reps):
+        _, kind, w = cpu_sample(wl, os.cpu_count() or 1, its)
+        wall += w
+    v = wl["W"] * wl["H"] * wl.get("D", 1) * its * reps / wall / 1e9
+    sample = f"{shape} grid, {reps} run(s) of {its} iterations (of {wl['iters']}), {wall:.2f} s"
+    if wl.get("batch"):
+        sample = f"one {shape} grid of the same stencil (the reference runs grid by grid), " + sample[len(shape) + 7:]
+    return {"value": round(v, 4), "unit": "GCells/s", "cores": os.cpu_count() or 1, "kind": kind, "sample": sample}
+
+
+def run_workload(name, args, world, rank, local, cpu_updates):
+    import torch
+    wl = dict(WORKLOADS[name], name=name)
+    runner = run_batch if wl.get("batch") else run_ours
+    line, clocks = runner(args, wl, world, rank, local)
+    line["clocks"] = clocks
+    finish_roofline(line, name, clocks, torch.cuda.get_device_properties(local).multi_processor_count)
+    if rank == 0 and cpu_updates:
+        line["cpu_baseline"] = cpu_baseline(wl, cpu_updates)
+    return line
+
+
+def compact(line):
+    """The keys of another workload's line that the headline line carries."""
+    out = {k: line[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "dtype", "config", "schedule",
+                                "gpu_launches", "roofline", "cpu_baseline", "clocks") if k in line}
+    out["plain"] = line["plain"].get("value") if isinstance(line.get("plain"), dict) else None
+    out["e2e"] = line["e2e"]["value"]
+    if "tuning" in line:
+        out["tuning"] = {k: line["tuning"][k] for k in ("learned_vs_exhaustive", "learned_vs_ga_plain",
+                                                        "learned_vs_best_uniform", "exhaustive_batch",
+                                                        "ga_plain_launches", "best_uniform", "results_identical")}
+    return out
 
 
 def main():
@@ -770,34 +879,29 @@ def main():
     ap.add_argument("--time-steps", type=int, default=0)
     ap.add_argument("--tile-h", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-others", action="store_true",
+                    help="only the chosen workload (by default a single-GPU run of the headline workload also "
+                         "measures every other workload, with at most 5 timed steps each, under `others`)")
     ap.add_argument("--save-model", default="", help="batch workloads: write the trained cost model here")
     args = ap.parse_args()
-    wl = dict(WORKLOADS[args.workload], name=args.workload)
     world, rank, local = dist_setup()
     if args.impl == "reference":
-        line = run_reference_arm(args, wl, world, rank)
+        line = run_reference_arm(args, dict(WORKLOADS[args.workload], name=args.workload), world, rank)
         if line is not None:
             print(json.dumps(line), flush=True)
         return
-    runner = run_batch if wl.get("batch") else run_ours
-    line, clocks = runner(args, wl, world, rank, local)
-    line["clocks"] = clocks
+    line = run_workload(args.workload, args, world, rank, local, 0 if args.no_cpu_baseline else 2e10)
+    if world == 1 and args.workload == "life" and not args.no_others and not args.time_steps and not args.tile_h:
+        import torch
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup = min(args.steps, 5), 3
+        others = {}
+        for name in OTHERS:
+            others[name] = compact(run_workload(name, sub, world, rank, local,
+                                                0 if args.no_cpu_baseline else 5e9))
+            torch.cuda.empty_cache()
+        line["others"] = others
     if rank == 0:
-        if not args.no_cpu_baseline:
-            # a bounded sample: runs of at most the workload's iterations (the
-            # whole workload when it is small, repeated up to 10 times)
-            total = sample_iters(wl)
-            its = min(wl["iters"], total)
-            reps = min(10, max(1, total // its))
-            shape = "x".join(str(v) for v in ([wl["H"], wl["W"]] + ([wl["D"]] if "D" in wl else [])))
-            kind, wall = None, 0.0
-            for _ in range(reps):
-                _, kind, w = cpu_sample(wl, os.cpu_count() or 1, its)
-                wall += w
-            v = wl["W"] * wl["H"] * wl.get("D", 1) * its * reps / wall / 1e9
-            line["cpu_baseline"] = {"value": round(v, 4), "unit": "GCells/s", "cores": os.cpu_count() or 1,
-                                    "kind": kind, "sample": f"{shape} grid, {reps} run(s) of {its} "
-                                                            f"iterations (of {wl['iters']}), {wall:.2f} s"}
         print(json.dumps(line), flush=True)
 
 

@@ -189,6 +189,55 @@ inline size_t device_budget() {
   return fr;
 }
 
+// Rows [lo, hi) of a host array (whole rows; whole h-planes in 3D), copied to
+// or from the device memory `dev`. A sliced array goes through its own
+// element-wise copy. Used by the out-of-core runs of user functors.
+template <class Array>
+void rows_to_device(const Array& a, size_t lo, size_t hi, typename Array::value_type* dev) {
+  typedef typename Array::value_type V;
+  const size_t row = a.getWidth() * a.getDepth();
+  if (a.contiguous()) {
+    gpuErrchk(cudaMemcpy(dev, a.hostArray + lo * row, (hi - lo) * row * sizeof(V), cudaMemcpyHostToDevice));
+    return;
+  }
+  Array s = a;
+  s.deviceArray = nullptr;  // never free the parent's device memory
+  s.hostSlice(a, 0, lo, 0, a.getWidth(), hi - lo, a.getDepth());
+  s.deviceArray = dev;
+  s.copyToDevice();
+}
+
+template <class Array>
+void rows_to_host(Array& a, size_t lo, size_t hi, const typename Array::value_type* dev) {
+  typedef typename Array::value_type V;
+  const size_t row = a.getWidth() * a.getDepth();
+  if (a.contiguous()) {
+    gpuErrchk(cudaMemcpy(a.hostArray + lo * row, dev, (hi - lo) * row * sizeof(V), cudaMemcpyDeviceToHost));
+    return;
+  }
+  Array s = a;
+  s.deviceArray = nullptr;
+  s.hostSlice(a, 0, lo, 0, a.getWidth(), hi - lo, a.getDepth());
+  Array src = s;
+  src.deviceArray = const_cast<V*>(dev);
+  s.copyFromDevice(src);
+}
+
+// Core rows of an out-of-core slab: the tiling height when given, else
+// the most that fit `budget` bytes as `buffers` device buffers of the slab
+// and its halo (90 % of the budget), at least one and at most `extent`.
+inline size_t slab_rows(size_t given, size_t budget, size_t row_bytes, size_t buffers, size_t halo_rows,
+                        size_t extent) {
+  size_t s = given;
+  if (s == 0) {
+    const size_t fit = budget > 0 ? (budget / 10 * 9) / (buffers * row_bytes) : extent;
+    s = fit > 2 * halo_rows ? fit - 2 * halo_rows : 1;
+  }
+  if (s < 1) s = 1;
+  if (s > extent) s = extent;
+  return s;
+}
+
 #ifdef __CUDACC__
 // ------------------------------------------------ user-functor GPU kernels
 
@@ -196,10 +245,14 @@ inline size_t device_budget() {
 // Same scheme as the library kernels: a (TW + 2RT) x (TH + 2RT) tile, a
 // shrinking computed region per step, tiles that reach the ring also stage
 // the destination's ring, the core written back for interior cells only.
+// The buffers hold H rows of the grid starting at grid row `row0` (0 for a
+// whole grid; a slab of an out-of-core run otherwise): the functor sees grid
+// coordinates, and the buffers' first and last `ring` rows are not updated
+// (the grid's ring, or a slab edge whose rows the caller does not keep).
 template <class Array, class Mask, class Args>
 __global__ void __launch_bounds__(256) functor2d_pass(Array in, Array out, Mask mask, Args args, int W, int H,
                                                       int ring, int R, int steps, int T, int TW, int TH,
-                                                      int tiles_x, int tiles_y) {
+                                                      int tiles_x, int tiles_y, int row0) {
   typedef typename Array::value_type V;
   typedef typename std::remove_reference<decltype(mask.getWeight(0))>::type WT;
   extern __shared__ __align__(16) unsigned char pskel_smem[];
@@ -233,7 +286,7 @@ __global__ void __launch_bounds__(256) functor2d_pass(Array in, Array out, Mask 
     Array va = in, vb = out;
     va.deviceArray = A;
     vb.deviceArray = B;
-    va.pskel_org_h = vb.pskel_org_h = gy0;
+    va.pskel_org_h = vb.pskel_org_h = gy0 + row0;
     va.pskel_org_w = vb.pskel_org_w = gx0;
     va.pskel_pitch_w = vb.pskel_pitch_w = LW;
     for (int s = 1; s <= steps; ++s) {
@@ -246,7 +299,7 @@ __global__ void __launch_bounds__(256) functor2d_pass(Array in, Array out, Mask 
         const int y = ylo + i / rw, x = xlo + i % rw;
         const int gy = gy0 + y, gx = gx0 + x;
         if (gy >= ring && gy < H - ring && gx >= ring && gx < W - ring)
-          stencilKernel(vin, vout, mask, args, static_cast<size_t>(gy), static_cast<size_t>(gx));
+          stencilKernel(vin, vout, mask, args, static_cast<size_t>(gy + row0), static_cast<size_t>(gx));
       }
       __syncthreads();
     }
@@ -268,12 +321,15 @@ __global__ void __launch_bounds__(256) functor1d_step(Array in, Array out, Mask 
     stencilKernel(in, out, mask, args, i);
 }
 
-// One step of a user functor on a 3D grid: every cell, d fastest across lanes.
+// One step of a user functor on a 3D grid: every cell of the planes
+// [h0, h1), d fastest across lanes (grid coordinates; an out-of-core slab
+// passes its own planes).
 template <class Array, class Mask, class Args>
-__global__ void __launch_bounds__(128) functor3d_step(Array in, Array out, Mask mask, Args args, int W, int H, int D) {
+__global__ void __launch_bounds__(128) functor3d_step(Array in, Array out, Mask mask, Args args, int W, int h0, int h1,
+                                                      int D) {
   const int d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= D) return;
-  for (int h = blockIdx.z; h < H; h += gridDim.z)
+  for (int h = h0 + static_cast<int>(blockIdx.z); h < h1; h += gridDim.z)
     for (int w = blockIdx.y; w < W; w += gridDim.y)
       stencilKernel(in, out, mask, args, static_cast<size_t>(h), static_cast<size_t>(w), static_cast<size_t>(d));
 }
@@ -441,9 +497,100 @@ class Stencil2D : public StencilBase<Array, Mask, Args> {
     if constexpr (op != kUserFunctor && dt >= 0) {
       runLibrary(iterations, detail::make_schedule(0, 0, 0, 0), true, slabRows, innerIterations, budget);
       return true;
+    } else {
+#ifdef __CUDACC__
+      runFunctorOutOfCore(iterations, slabRows, innerIterations, budget);
+      return true;
+#else
+      (void)iterations;
+      (void)slabRows;
+      (void)innerIterations;
+      (void)budget;
+      return false;
+#endif
     }
-    return false;
   }
+
+#ifdef __CUDACC__
+  // A user functor on arrays larger than the device memory: the reference's
+  // host tiling (runIterativeTilingGPU, PSkelStencil.hpp:1663-1760) with
+  // full-width slabs of `slabRows` core rows (sized from the budget when 0)
+  // and `innerIterations` steps per visit. Each pass (odd length, so every
+  // step sees the ring the step-by-step run sees) reads one host array and
+  // writes the other: per slab, the source and destination rows of the slab
+  // and a halo of R x steps rows go to the device, the generated tile kernel
+  // runs the pass on them with grid coordinates (rows beyond the slab's halo
+  // are never read; the halo absorbs what its edge rows get wrong), and the
+  // slab's core rows come back. As in the reference, the passes ping-pong
+  // between a host copy of the input and the output, and the input array is
+  // left as it was.
+  void runFunctorOutOfCore(size_t iterations, size_t slabRows, size_t innerIterations, size_t budget) {
+    const int W = static_cast<int>(this->input.getWidth()), H = static_cast<int>(this->input.getHeight());
+    const int ring = static_cast<int>(this->mask.getRange());
+    const int reach = static_cast<int>(this->mask.maxOffset());
+    const int R = ring > reach ? ring : reach;
+    int TB = innerIterations > 0 ? static_cast<int>(innerIterations) : 5;
+    if (R == 0) TB = 1;
+    std::vector<int32_t> passes(static_cast<size_t>(iterations) + 1);
+    const int np = pskel_plan_passes(static_cast<int64_t>(iterations), TB, passes.data(),
+                                     static_cast<int32_t>(passes.size()));
+    TB = 1;
+    for (int i = 0; i < np; ++i) TB = passes[i] > TB ? passes[i] : TB;
+    const size_t halo = static_cast<size_t>(R) * TB;
+    const size_t S = detail::slab_rows(slabRows, budget, static_cast<size_t>(W) * sizeof(T), 2, halo,
+                                       static_cast<size_t>(H));
+    const size_t cap = S + 2 * halo < static_cast<size_t>(H) ? S + 2 * halo : static_cast<size_t>(H);
+    T* din = nullptr;
+    T* dout = nullptr;
+    gpuErrchk(cudaMalloc(reinterpret_cast<void**>(&din), cap * W * sizeof(T)));
+    gpuErrchk(cudaMalloc(reinterpret_cast<void**>(&dout), cap * W * sizeof(T)));
+    this->mask.deviceAlloc();
+    this->mask.copyToDevice();
+    const int TW = 64, TH = 32;
+    typedef typename std::remove_reference<decltype(this->mask.getWeight(0))>::type WT;
+    const size_t tile_bytes =
+        ((static_cast<size_t>(TW + 2 * R * TB) * (TH + 2 * R * TB) * sizeof(T)) + 15) & ~size_t(15);
+    const size_t smem = 2 * tile_bytes + ((this->mask.size * this->mask.dimension + 3) & ~size_t(3)) * sizeof(int) +
+                        this->mask.size * sizeof(WT) + 16;
+    auto kern = detail::functor2d_pass<Array, Mask, Args>;
+    gpuErrchk(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int dev = 0, sms = 0, per_sm = 0;
+    gpuErrchk(cudaGetDevice(&dev));
+    gpuErrchk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    gpuErrchk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+    Array copy;
+    copy.hostClone(this->input);  // the reference's inputCopy: the input array is not written
+    for (int i = 0; i < np; ++i) {
+      Array& src = (i % 2 == 0) ? copy : this->output;
+      Array& dst = (i % 2 == 0) ? this->output : copy;
+      for (size_t c0 = 0; c0 < static_cast<size_t>(H); c0 += S) {
+        const size_t c1 = c0 + S < static_cast<size_t>(H) ? c0 + S : static_cast<size_t>(H);
+        const size_t lo = c0 > halo ? c0 - halo : 0;
+        const size_t hi = c1 + halo < static_cast<size_t>(H) ? c1 + halo : static_cast<size_t>(H);
+        const int Hs = static_cast<int>(hi - lo);
+        detail::rows_to_device(src, lo, hi, din);
+        detail::rows_to_device(dst, lo, hi, dout);  // its ring is read by every second step
+        Array vin = src, vout = dst;
+        vin.deviceArray = din;
+        vout.deviceArray = dout;
+        const int tiles_x = (W + TW - 1) / TW, tiles_y = (Hs + TH - 1) / TH;
+        int ctas = (per_sm > 0 ? per_sm : 1) * sms;
+        if (ctas > tiles_x * tiles_y) ctas = tiles_x * tiles_y;
+        kern<<<ctas, 256, smem>>>(vin, vout, this->mask, this->args, W, Hs, ring, R, passes[i], TB, TW, TH, tiles_x,
+                                  tiles_y, static_cast<int>(lo));
+        gpuErrchk(cudaPeekAtLastError());
+        detail::rows_to_host(dst, c0, c1, dout + (c0 - lo) * W);
+      }
+    }
+    // an even number of passes ends in the copy (with the input's ring, as the
+    // step-by-step run leaves it)
+    if (np % 2 == 0) this->output.hostMemCopy(copy);
+    copy.hostFree();
+    gpuErrchk(cudaFree(din));
+    gpuErrchk(cudaFree(dout));
+    this->mask.deviceFree();
+  }
+#endif
 
   void runLibrary(size_t iterations, pskel_schedule sched, bool tiled = false, size_t slabRows = 0,
                   size_t innerIterations = 0, size_t budget = 0) {
@@ -522,7 +669,7 @@ class Stencil2D : public StencilBase<Array, Mask, Args> {
     for (int i = 0; i < np; ++i) {
       const bool fwd = (i % 2 == 0);
       kern<<<ctas, 256, smem>>>(fwd ? in : out, fwd ? out : in, this->mask, this->args, W, H, ring, R, passes[i], TB,
-                                TW, TH, tiles_x, tiles_y);
+                                TW, TH, tiles_x, tiles_y, 0);
       gpuErrchk(cudaPeekAtLastError());
     }
     gpuErrchk(cudaDeviceSynchronize());
@@ -666,13 +813,83 @@ class Stencil3D : public StencilBase<Array, Mask, Args> {
                                          nullptr));
       out.write_back();
       return true;
+    } else {
+#ifdef __CUDACC__
+      runFunctorOutOfCore(iterations, slabRows, innerIterations, budget);
+      return true;
+#else
+      (void)iterations;
+      (void)slabRows;
+      (void)innerIterations;
+      (void)budget;
+      return false;
+#endif
     }
-    (void)iterations;
-    (void)slabRows;
-    (void)innerIterations;
-    (void)budget;
-    return false;
   }
+
+#ifdef __CUDACC__
+  // A user functor on 3D arrays larger than the device memory: slabs of
+  // `slabRows` h-planes (sized from the budget when 0) with a halo of
+  // R x steps planes, `innerIterations` steps per visit (the reference's host
+  // tiling, PSkelStencil.hpp:1663-1760, in full (w, d) planes). Every cell is
+  // updated each step (Stencil3D semantics); the slab buffers carry R guard
+  // planes on each side so that the functor's reads through Mask3D::get at
+  // the slab's edge planes stay inside them (those planes are halo: the
+  // values they get are not kept). The passes ping-pong between a host copy
+  // of the input and the output; the input array is left as it was.
+  void runFunctorOutOfCore(size_t iterations, size_t slabRows, size_t innerIterations, size_t budget) {
+    const int W = static_cast<int>(this->input.getWidth()), H = static_cast<int>(this->input.getHeight());
+    const int D = static_cast<int>(this->input.getDepth());
+    const int R = static_cast<int>(this->mask.maxOffset());
+    const int TB = innerIterations > 0 ? static_cast<int>(innerIterations) : 4;
+    const size_t plane = static_cast<size_t>(W) * D;
+    const size_t halo = static_cast<size_t>(R) * TB, G = static_cast<size_t>(R);
+    const size_t S = detail::slab_rows(slabRows, budget, plane * sizeof(T), 2, halo + G, static_cast<size_t>(H));
+    const size_t cap = (S + 2 * halo < static_cast<size_t>(H) ? S + 2 * halo : static_cast<size_t>(H)) + 2 * G;
+    T* buf[2] = {nullptr, nullptr};
+    for (T*& b : buf) {
+      gpuErrchk(cudaMalloc(reinterpret_cast<void**>(&b), cap * plane * sizeof(T)));
+      gpuErrchk(cudaMemset(b, 0, cap * plane * sizeof(T)));
+    }
+    this->mask.deviceAlloc();
+    this->mask.copyToDevice();
+    Array copy;
+    copy.hostClone(this->input);  // the reference's inputCopy: the input array is not written
+    const dim3 block(128);
+    size_t np = 0;
+    for (size_t done = 0; done < iterations; ++np) {
+      const int steps = static_cast<int>(iterations - done < static_cast<size_t>(TB) ? iterations - done : TB);
+      Array& src = (np % 2 == 0) ? copy : this->output;
+      Array& dst = (np % 2 == 0) ? this->output : copy;
+      for (size_t c0 = 0; c0 < static_cast<size_t>(H); c0 += S) {
+        const size_t c1 = c0 + S < static_cast<size_t>(H) ? c0 + S : static_cast<size_t>(H);
+        const size_t lo = c0 > halo ? c0 - halo : 0;
+        const size_t hi = c1 + halo < static_cast<size_t>(H) ? c1 + halo : static_cast<size_t>(H);
+        detail::rows_to_device(src, lo, hi, buf[0] + G * plane);
+        const int Hs = static_cast<int>(hi - lo);
+        const dim3 grid((D + 127) / 128, W < 65535 ? W : 65535, Hs < 65535 ? Hs : 65535);
+        for (int s = 0; s < steps; ++s) {
+          // views with grid coordinates: plane h sits at buffer plane h - lo + G
+          Array vin = src, vout = dst;
+          vin.deviceArray = buf[s % 2] + G * plane;
+          vout.deviceArray = buf[(s + 1) % 2] + G * plane;
+          vin.reset_view();
+          vout.reset_view();
+          vin.pskel_org_h = vout.pskel_org_h = static_cast<long>(lo);
+          detail::functor3d_step<<<grid, block>>>(vin, vout, this->mask, this->args, W, static_cast<int>(lo),
+                                                  static_cast<int>(hi), D);
+          gpuErrchk(cudaPeekAtLastError());
+        }
+        detail::rows_to_host(dst, c0, c1, buf[steps % 2] + (G + c0 - lo) * plane);
+      }
+      done += static_cast<size_t>(steps);
+    }
+    if (np % 2 == 0) this->output.hostMemCopy(copy);
+    copy.hostFree();
+    for (T* b : buf) gpuErrchk(cudaFree(b));
+    this->mask.deviceFree();
+  }
+#endif
 
   void runGPUSchedule(size_t iterations, pskel_schedule sched) override {
     constexpr int op = StencilOp<Args>::value;
@@ -712,9 +929,9 @@ class Stencil3D : public StencilBase<Array, Mask, Args> {
     const dim3 grid((D + 127) / 128, W < 65535 ? W : 65535, H < 65535 ? H : 65535);
     for (size_t it = 0; it < iterations; ++it) {
       if (it % 2 == 0)
-        detail::functor3d_step<<<grid, block>>>(in, out, this->mask, this->args, W, H, D);
+        detail::functor3d_step<<<grid, block>>>(in, out, this->mask, this->args, W, 0, H, D);
       else
-        detail::functor3d_step<<<grid, block>>>(out, in, this->mask, this->args, W, H, D);
+        detail::functor3d_step<<<grid, block>>>(out, in, this->mask, this->args, W, 0, H, D);
       gpuErrchk(cudaPeekAtLastError());
     }
     gpuErrchk(cudaDeviceSynchronize());

@@ -17,7 +17,10 @@ This script therefore:
      directory; nothing of the reference is committed),
   2. wraps exactly those three line ranges of the copy in ``#ifdef PSKEL_CUDA``
      after checking the sha256 of the original file, so a different reference
-     revision is refused instead of being patched blindly,
+     revision is refused instead of being patched blindly, and qualifies the
+     two device accesses of lines 345 and 642 (``width``/``depth`` of a
+     dependent base) with ``this->`` so the copy also compiles under nvcc with
+     ``PSKEL_CUDA`` (used only to show that user code compiles against it),
   3. writes two shim headers (``tbb/scalable_allocator.h`` over malloc/free and
      ``xmmintrin.h`` over posix_memalign, which also makes the build portable
      to aarch64 hosts),
@@ -25,8 +28,8 @@ This script therefore:
      ``g++ -O3 -ffp-contract=off -fopenmp -DPSKEL_OMP`` into
      ``oracle/_ref/pskel_ref``.
 
-Step 1-3 need the reference tree (default ``/root/reference``, or the
-``PSKEL_REFERENCE`` environment variable). Step 4 only needs ``oracle/_ref/src``,
+Step 1-3 need the reference tree (the ``PSKEL_REFERENCE`` environment
+variable, else a ``reference`` directory beside this repository's root). Step 4 only needs ``oracle/_ref/src``,
 so on a machine without the reference the previously prepared copy is compiled.
 """
 from __future__ import annotations
@@ -48,6 +51,8 @@ BIN = OUT / "pskel_ref"
 ARRAY_HPP_SHA256 = "eee8c8e0c3e492be63452c199138c7b73d5ac7af7b0a2e8527e2e8d8c6d06fe6"
 # 1-based inclusive line ranges of PSkelArray.hpp that only make sense with CUDA.
 CUDA_ONLY_RANGES = [(209, 230), (278, 284), (501, 509)]
+# 1-based lines of PSkelArray.hpp whose device access needs this-> qualified members.
+UNQUALIFIED_LINES = [345, 642]
 
 SHIM_TBB = """// Shim for the oracle build: PSkel.h includes this header unconditionally.
 #pragma once
@@ -70,7 +75,10 @@ inline void _mm_free(void* p) { std::free(p); }
 
 
 def reference_include() -> Path | None:
-    root = Path(os.environ.get("PSKEL_REFERENCE", "/root/reference"))
+    """The reference's include/ directory: $PSKEL_REFERENCE, else a checkout
+    named ``reference`` next to this repository (the build layout here)."""
+    env = os.environ.get("PSKEL_REFERENCE")
+    root = Path(env) if env else HERE.parent.parent / "reference"
     inc = root / "include"
     return inc if (inc / "PSkelStencil.hpp").is_file() else None
 
@@ -88,6 +96,15 @@ def prepare_overlay(inc: Path) -> None:
         raise RuntimeError(f"unexpected PSkelArray.hpp revision (sha256 {digest}); "
                            "line ranges of the overlay were read from another revision")
     lines = raw.decode("latin-1").split("\n")
+    # Array::operator() and Array3D::operator() (lines 345 and 642) name the
+    # dependent base members width/depth without this->, which nvcc rejects
+    # once PSKEL_CUDA compiles the device branch: qualify them, nothing else.
+    unq = "return this->deviceArray[(h*width+w)*depth+d];"
+    hits = [i for i, l in enumerate(lines) if l.strip() == unq]
+    if [i + 1 for i in hits] != UNQUALIFIED_LINES:
+        raise RuntimeError(f"unexpected PSkelArray.hpp: unqualified device accesses at {[i + 1 for i in hits]}")
+    for i in hits:
+        lines[i] = lines[i].replace(unq, "return this->deviceArray[(h*this->width+w)*this->depth+d];")
     for lo, hi in sorted(CUDA_ONLY_RANGES, reverse=True):
         lines.insert(hi, "#endif /* oracle overlay */")
         lines.insert(lo - 1, "#ifdef PSKEL_CUDA /* oracle overlay */")

@@ -4,8 +4,9 @@ This Python module is a thin ctypes binding of the C ABI in
 ``include/pskel_gb300.h`` (the library ``pskel_gb300/libpskel_gb300.so``),
 used by the tests and the benchmark. C++ applications use the drop-in headers
 ``include/PSkel*.h`` instead. There is no CPU fallback: every call runs the
-CUDA kernels of the library, and importing this module raises if the library
-has not been built.
+CUDA kernels of the library. The library is opened on first use (so that
+the seeded input generators in ``pskel_gb300.synth`` import without it), and
+that first use raises if the library has not been built.
 """
 from __future__ import annotations
 
@@ -87,7 +88,27 @@ def _load():
     return lib
 
 
-lib = _load()
+class _Lib:
+    """The library, opened on first use: importing the package (for example
+    only for ``pskel_gb300.synth``, the seeded input generators) maps no
+    native code, and the first call raises ImportError if the library has not
+    been built -- there is no other path to fall back to."""
+
+    _cdll = None
+
+    def __getattr__(self, name):
+        if _Lib._cdll is None:
+            _Lib._cdll = _load()
+        return getattr(_Lib._cdll, name)
+
+
+lib = _Lib()
+
+
+def load():
+    """Opens the library now (raises ImportError if it is missing)."""
+    lib.pskel_version()
+    return _Lib._cdll
 
 
 def _check(status: int):

@@ -9,7 +9,8 @@
 // CTA waits until all tiles of pass r-1 of the same grid have been written
 // (a per-grid completion counter); every such tile was taken earlier by a
 // resident CTA, so the wait always ends. It is still bounded: after
-// kBatchSpinLimit polls the CTA latches kDevErrBarrier and stops.
+// kBatchSpinLimit polls the CTA latches kDevErrBarrier and stops, and every
+// other CTA stops at its next poll or item once it sees the latched word.
 //
 // Each tile is processed by the register-windowed tile routine of the
 // single-grid kernel (fast2d_tile.cuh): TMA-staged source tile, destination
@@ -56,9 +57,6 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-__device__ __forceinline__ void fence_proxy_async_global() {
-  asm volatile("fence.proxy.async.global;" ::: "memory");
-}
 
 template <class TS, int OpK, int S>
 __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
@@ -95,7 +93,7 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
 
   for (;;) {
     if (tid == 0) {
-      const int64_t item = static_cast<int64_t>(atomicAdd(next_item, 1ull));
+      const int64_t item = error_latched(bp.err) ? nitems : static_cast<int64_t>(atomicAdd(next_item, 1ull));
       s_item = item;
       if (item < nitems) {
         int lo = 0, hi = nsegs - 1;  // last segment with start <= item
@@ -126,6 +124,10 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
         const unsigned target = static_cast<unsigned>(seg.pass) * static_cast<unsigned>(G.ntiles);
         unsigned polls = 0;
         while (ld_acquire(&done[seg.g]) < target) {
+          if (error_latched(bp.err)) {  // another CTA gave up and reported why
+            ok = 0;
+            break;
+          }
           if (++polls >= kBatchSpinLimit) {
             atomicOr(bp.err, kDevErrBarrier);
             ok = 0;

@@ -221,6 +221,9 @@ static bool tma_ok(const void* p, int64_t pitch_bytes) {
 // planes (L2-resident for grids up to ~16k x 16k), the passes run between the
 // planes, and the final plane's interior is unpacked into the result buffer.
 // The other buffer is not written; ring cells of the result keep their bytes.
+// Generations per pass of the Life kernel by default (measured on GB300, 8192^2).
+constexpr int kLifeDefaultSteps = 15;
+
 static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
                                  int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,
                                  cudaStream_t s) {
@@ -233,8 +236,8 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
   auto geom_for = [&](int T, Geo& g) -> bool {
     T = static_cast<int>(std::min<int64_t>(std::min(T, kLifeBitsMaxT), it1));
     if (T > 1 && (T & 1) == 0) --T;  // passes have odd lengths (plan_passes)
-    int TH = (sched && sched->tile_h > 0) ? sched->tile_h : 256 - 2 * T;
-    TH = std::min(TH, 256 - 2 * T);
+    int TH = (sched && sched->tile_h > 0) ? sched->tile_h : life_bits_max_tile_h(T);
+    TH = std::min(TH, life_bits_max_tile_h(T));
     if (TH < 1) return false;
     g.T = T;
     g.TH = TH;
@@ -245,10 +248,8 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
     if (!geom_for(sched->time_steps, g))
       return fail(PSKEL_ERR_INVALID, "Life tile height too small for %d steps per pass", sched->time_steps);
   } else {
-    // Default: 25 generations per pass on full-height tiles (256 loaded rows),
-    // the fastest measured on GB300 (8192^2: 22.4 T updates/s; 15: 21.0,
-    // 21: 21.9, 31: 21.4)
-    if (!geom_for(25, g) && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
+    // Default: kLifeDefaultSteps generations per pass on full-height tiles
+    if (!geom_for(kLifeDefaultSteps, g) && !geom_for(1, g)) return fail(PSKEL_ERR_INVALID, "no Life geometry fits");
   }
   const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), g.TH);
   // every pass in one persistent launch: no more CTAs than can be resident
@@ -955,13 +956,13 @@ constexpr int kLifeWavePasses = 4;
 static pskel_status run_life_host_wavefront(const uint8_t* in_host, uint8_t* out_host, int64_t W, int64_t H,
                                             int64_t iters, int ring, int steps, DeviceContext* c, bool* used) {
   *used = false;
-  int T = static_cast<int>(std::min<int64_t>(std::min(steps > 0 ? steps : 25, kLifeBitsMaxT), iters));
+  int T = static_cast<int>(std::min<int64_t>(std::min(steps > 0 ? steps : kLifeDefaultSteps, kLifeBitsMaxT), iters));
   if (T > 1 && (T & 1) == 0) --T;
-  const int TH = 256 - 2 * T;
+  const int TH = life_bits_max_tile_h(T);
   const std::vector<int> passes = plan_passes(iters, T);
   const int P = static_cast<int>(passes.size());
   const int tiles_y = static_cast<int>((H + TH - 1) / TH);
-  const int tiles_x = (life_bits_words(static_cast<int>(W)) + 13) / 14;
+  const int tiles_x = life_bits_tiles_x(static_cast<int>(W));
   if (P < 2 || tiles_y < 4 * kLifeChunks || H >= (int64_t(1) << 30)) return PSKEL_OK;
   *used = true;
   const int q = (passes.back() - 1) / 2;

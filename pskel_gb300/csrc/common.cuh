@@ -17,6 +17,19 @@ enum DeviceError : unsigned {
   kDevErrAlign = 8u,      // dynamic shared memory not 128-byte aligned (kernel did nothing)
 };
 
+// Bits after which the persistent kernels stop: a wait that ran out means a
+// producer never arrived, and every item that depends on it would wait its
+// full limit too. (kDevErrValue is only reported.)
+constexpr unsigned kDevErrStop = kDevErrTimeout | kDevErrBarrier;
+
+// True once a stop bit is latched in the error word (by this launch or an
+// earlier one of the call): persistent kernels then take no more items and
+// abandon their dependency waits, so one lost tile costs one wait limit, not
+// one per dependent item.
+__device__ __forceinline__ bool error_latched(const unsigned* err) {
+  return (*reinterpret_cast<const volatile unsigned*>(err) & kDevErrStop) != 0u;
+}
+
 // Upper bound on mbarrier polls before a kernel gives up on a TMA load. A load
 // of one tile completes in microseconds; 2^26 polls is seconds.
 constexpr unsigned kMbarSpinLimit = 1u << 26;
@@ -35,6 +48,16 @@ __device__ __forceinline__ void fence_barrier_init() {
 
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Orders this thread's earlier generic-proxy accesses of global memory (and
+// those it has observed) before its later async-proxy (TMA) accesses.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {

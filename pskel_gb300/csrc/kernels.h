@@ -23,10 +23,20 @@ std::vector<int> plan_passes(int64_t iters, int T);
 
 // Bit-plane Life: pack both grids once into global bit planes (rows of
 // life_bits_words(W) words), run the passes between the planes, unpack the
-// final plane's interior into the result buffer. Tiles: 16 words x (TH + 2T)
-// rows with one word and T rows of halo, T <= kLifeBitsMaxT.
+// final plane's interior into the result buffer. A tile is one warp of words
+// wide (kLifeCoreWords core words, one halo word each side) and holds a
+// window of kLifeWindowRows rows in registers (kLifeWarps consumer warps x
+// kLifeRows rows, plus one row above and below); after T <= kLifeBitsMaxT
+// steps its core of TH <= life_bits_max_tile_h(T) = kLifeWindowRows - 2T rows
+// is exact.
 constexpr int kLifeBitsMaxT = 31;
+constexpr int kLifeRows = 8;
+constexpr int kLifeWarps = 15;
+constexpr int kLifeCoreWords = 30;
+constexpr int kLifeWindowRows = kLifeWarps * kLifeRows + 2;
 int life_bits_words(int W);
+int life_bits_tiles_x(int W);
+int life_bits_max_tile_h(int T);
 size_t life_bits_smem_bytes();
 int life_bits_tiles(int W, int H, int TH);
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
@@ -51,8 +61,10 @@ struct LifeWindow {
   long long start[kLifeMaxWindow + 1];
 };
 cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t s);
+// restart: clear the item counter first (the completion counts carry over)
 cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int ring, const LifeWindow& win, int q,
-                                 int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s);
+                                 int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s,
+                                 bool restart = true);
 // Pack rows [row0, row1) (every cell checked to be 0/1) / unpack the interior
 // cells of rows [row0, row1).
 cudaError_t life_bits_pack_rows(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring,

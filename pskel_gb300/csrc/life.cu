@@ -3,28 +3,39 @@
 // A run packs the source and destination grids (one 0/1 byte per cell, the
 // reference's layout) once into two global bit planes -- one bit per cell,
 // 16 MB for an 8192^2 grid, so the planes stay in L2 -- runs every pass
-// between the planes and unpacks the final plane's interior into the result
-// buffer once. A pass advances the grid by up to 31 steps: each persistent
-// CTA walks tiles of 14 x 32 core columns and TH core rows, stages the
-// 16-word x (TH + 2T)-row halo tile into a shared bit plane with cp.async,
-// runs the steps there (neighbour counts with bit-sliced full adders: 32
-// cells per word and about a dozen LOP3/funnel-shift operations per word and
-// step) and writes the core words back. Ring cells (outside r <= h < H-r,
-// r <= w < W-r) are never updated, the semantics of Stencil2D::runOpenMP
-// (PSkelStencil.hpp:2197-2257): tiles that reach the ring also stage the
-// destination plane's tile, whose ring bits the odd steps read and the
-// write-back keeps.
+// between the planes in one persistent launch and unpacks the final plane's
+// interior into the result buffer once.
 //
-// Redundant halo work: the tile carries T rows and 32 columns of halo on each
-// side; garbage entering from the tile edge advances one cell per step, so
-// the core is exact after T <= 31 steps.
+// A pass advances a tile by up to 31 steps with the tile held in registers:
+// one warp spans 32 words (1024 cells) of a tile row, lane l holding word
+// 30*tx - 1 + l (lanes 1..30 are the tile's core, lanes 0 and 31 its one-word
+// halo), and each lane holds a column of kLifeRows words of its warp's rows
+// plus a copy of the row above and below. West/east neighbour words come
+// from the adjacent lanes by warp shuffles, rows above/below from the
+// lane's own registers; after each step the warps of a block exchange their
+// first and last rows through shared memory. A step costs per 32-cell word
+// 2 shuffles, 2 funnel shifts and 10 LOP3s (row sums shared by the three rows
+// that use them, bit-sliced full adders). Tiles are staged straight from L2
+// into registers with 32-bit ld.global.cg (one load per word per pass:
+// there is no shared-memory copy of the tile to stage into).
+//
+// Ring cells (outside r <= h < H-r, r <= w < W-r) are never updated, the
+// semantics of Stencil2D::runOpenMP (PSkelStencil.hpp:2197-2257): in the
+// step-by-step run a ring cell holds the source buffer's value after even
+// steps and the destination buffer's after odd ones. Tiles that reach the
+// ring therefore keep, per word, the interior mask M and the flip
+// D = (src ^ dst) outside M in shared memory, and a step writes
+// M ? rule : old ^ D.
+//
+// Redundant halo work: garbage enters a tile at its outermost rows (never
+// refreshed) and at lanes 0 and 31 (no neighbour lane) and advances one cell
+// per step, so after T <= 31 steps rows T .. T + TH - 1 of the window and
+// lanes 1..30 are exact.
 #include "common.cuh"
 #include "kernels.h"
 
 namespace pskel {
 namespace {
-
-constexpr int kRowsPerStrip = 8;  // rows of one word column a thread steps
 
 // 16 cells (one byte each, value 0/1) -> 16 bits, cell i at bit i.
 __device__ __forceinline__ uint32_t pack16(uint4 v) {
@@ -68,67 +79,67 @@ constexpr uint32_t kNotAAndBxC = 0x06;  // ~a & (b ^ c)
 constexpr uint32_t kAAndBorC = 0xE0;  // a & (b | c)
 constexpr uint32_t kSelect = 0xCA;    // a ? b : c, bitwise
 
-// One step for a strip of 8 rows of one word column. The neighbour count of
-// each cell is (w + c + e of the row above) + (w + e of its row) + (w + c + e
-// of the row below); each term is a 2-bit bit-sliced number, and the three are
-// added with full adders: s0 = low bit, k0 = its carry, x1/y1 = sum/carry of
-// the twos. With k0 folded in, count in {2, 3} <=> ~y1 & (x1 ^ k0), and the
-// cell lives iff that holds and (s0 | alive): count 3, or count 2 and alive.
-// A count of 8 leaves y1 set, so it is dead as it must be.
-// P: the bit plane's row pitch in words (a zero row above row 0 and a zero
-// word left of word 0, so word (row, j) sits at (row + 1) * P + j + 1).
-template <bool kMasked, int P>
-__device__ __forceinline__ void life_strip(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int y0, int j,
-                                           uint32_t colmask, int gy0, int ring, int H) {
-  uint32_t c[kRowsPerStrip + 2], t0[kRowsPerStrip + 2], t1[kRowsPerStrip + 2];
-  uint32_t p0[kRowsPerStrip + 2], p1[kRowsPerStrip + 2];
-  const uint32_t* base = in + (y0 * P + j + 1);  // row y0 - 1
-#pragma unroll
-  for (int k = 0; k < kRowsPerStrip + 2; ++k) {
-    const uint32_t* r = base + k * P;
-    const uint32_t l = r[-1], cc = r[0], e = r[1];
-    const uint32_t we = __funnelshift_l(l, cc, 1);  // bit b = cell b-1
-    const uint32_t ea = __funnelshift_r(cc, e, 1);  // bit b = cell b+1
-    c[k] = cc;
-    t0[k] = lop3<kXor3>(we, cc, ea);
-    t1[k] = lop3<kMaj>(we, cc, ea);
-    p0[k] = we ^ ea;
-    p1[k] = we & ea;
-  }
-  uint32_t* o = out + ((y0 + 1) * P + j + 1);
-#pragma unroll
-  for (int k = 1; k <= kRowsPerStrip; ++k) {
-    const uint32_t s0 = lop3<kXor3>(t0[k - 1], p0[k], t0[k + 1]);
-    const uint32_t k0 = lop3<kMaj>(t0[k - 1], p0[k], t0[k + 1]);
-    const uint32_t x1 = lop3<kXor3>(t1[k - 1], p1[k], t1[k + 1]);
-    const uint32_t y1 = lop3<kMaj>(t1[k - 1], p1[k], t1[k + 1]);
-    const uint32_t two_or_three = lop3<kNotAAndBxC>(y1, x1, k0);
-    const uint32_t alive = lop3<kAAndBorC>(two_or_three, s0, c[k]);
-    uint32_t* dst = o + (k - 1) * P;
-    if (kMasked) {
-      // cells outside r <= h < H-r, r <= w < W-r keep the value this plane holds
-      const int gy = gy0 + y0 + k - 1;
-      const uint32_t m = (gy >= ring && gy < H - ring) ? colmask : 0u;
-      *dst = lop3<kSelect>(m, alive, *dst);
-    } else {
-      *dst = alive;
-    }
-  }
+// Register-resident tile geometry (kernels.h: kLifeRows, kLifeWarps,
+// kLifeCoreWords): consumer warp w of a block holds rows w*kLifeRows ..
+// w*kLifeRows + kLifeRows + 1 of the tile's window of kLifeWindowRows rows.
+static_assert(kLifeCoreWords == 30, "a tile is one warp of words with one halo word each side");
+
+// Row sums of one row for the bit-sliced neighbour count: with we / ea the
+// west / east neighbour of every cell (the adjacent lanes' words by shuffles,
+// bit b of `we` = cell b-1), (t0, t1) = we + c + ea and (p0, p1) = we + ea as
+// 2-bit bit-sliced numbers.
+__device__ __forceinline__ void row_sums(uint32_t c, uint32_t& t0, uint32_t& t1, uint32_t& p0, uint32_t& p1) {
+  const uint32_t l = __shfl_up_sync(0xFFFFFFFFu, c, 1);    // lane 0 gets its own word: halo lane
+  const uint32_t e = __shfl_down_sync(0xFFFFFFFFu, c, 1);  // lane 31 likewise
+  const uint32_t we = __funnelshift_l(l, c, 1);            // (c << 1) | (l >> 31)
+  const uint32_t ea = __funnelshift_r(c, e, 1);            // (c >> 1) | (e << 31)
+  t0 = lop3<kXor3>(we, c, ea);
+  t1 = lop3<kMaj>(we, c, ea);
+  p0 = we ^ ea;
+  p1 = we & ea;
 }
 
-// ---------------------------------------------------------------------------
-// Bit-plane passes. A run packs the source and destination grids once into
-// two global bit planes (one bit per cell, rows of PW words), runs every pass
-// between the planes -- 16 MB for an 8192^2 grid, resident in L2 -- and
-// unpacks the final plane into the result buffer's interior once. A pass
-// tile is 16 words (512 cells) x LH rows with one word (32 cells) and T rows
-// of halo on each side, staged by cp.async into a shared bit plane.
-constexpr int kBW = 16;                          // words per loaded tile row
-constexpr int kBCore = kBW - 2;                  // core words
-constexpr int kBP = kBW + 2;                     // shared plane pitch (zero word each side)
-constexpr int kBRows = 256;
-constexpr int kBPlane = (kBRows + 2) * kBP;      // words per shared plane
-constexpr int kBThreads = kBW * (kBRows / kRowsPerStrip);  // 512: a word column x an 8-row strip each
+// One step of a warp's rows 1..kLifeRows from rows 0..kLifeRows+1, in place.
+// The neighbour count of a cell is (row above: t) + (its row: p) + (row
+// below: t); the three 2-bit numbers are added with full adders: s0 = low
+// bit, k0 = its carry, x1/y1 = sum/carry of the twos. With k0 folded in,
+// count in {2, 3} <=> ~y1 & (x1 ^ k0), and the cell lives iff that holds and
+// (s0 | alive): count 3, or count 2 and alive. A count of 8 leaves y1 set,
+// so it is dead as it must be. kRing: cells outside the interior mask M of
+// the row take old ^ D instead (M, D per row and lane in shared memory).
+template <bool kRing>
+__device__ __forceinline__ void life_reg_step(uint32_t (&x)[kLifeRows + 2], const uint32_t* __restrict__ Mw,
+                                              const uint32_t* __restrict__ Dw, int lane) {
+  uint32_t a0, a1, u0, u1, b0, b1, q0, q1;
+  row_sums(x[0], a0, a1, u0, u1);
+  row_sums(x[1], b0, b1, q0, q1);
+#pragma unroll
+  for (int i = 1; i <= kLifeRows; ++i) {
+    uint32_t c0, c1, r0, r1;
+    row_sums(x[i + 1], c0, c1, r0, r1);  // row i+1 still holds the previous step
+    const uint32_t s0 = lop3<kXor3>(a0, q0, c0);
+    const uint32_t k0 = lop3<kMaj>(a0, q0, c0);
+    const uint32_t x1 = lop3<kXor3>(a1, q1, c1);
+    const uint32_t y1 = lop3<kMaj>(a1, q1, c1);
+    const uint32_t two_or_three = lop3<kNotAAndBxC>(y1, x1, k0);
+    const uint32_t alive = lop3<kAAndBorC>(two_or_three, s0, x[i]);
+    if (kRing) {
+      const uint32_t m = Mw[(i - 1) * 32 + lane];
+      const uint32_t d = Dw[(i - 1) * 32 + lane];
+      x[i] = lop3<kSelect>(m, alive, x[i] ^ d);
+    } else {
+      x[i] = alive;
+    }
+    a0 = b0;
+    a1 = b1;
+    b0 = c0;
+    b1 = c1;
+    q0 = r0;
+    q1 = r1;
+  }
+  (void)u0;
+  (void)u1;
+}
 
 // packs rows of `src` (bytes 0/1) into a bit plane; check: 0 = every cell must
 // be 0/1, 1 = only the ring (the interior of a destination is overwritten
@@ -215,130 +226,233 @@ __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) {
   return v;
 }
 
+// A block is kLifeWarps consumer warps, which hold and step the tile, and one
+// producer warp, which fetches the next work item, waits for its
+// dependencies and loads its window by TMA into shared memory while the
+// consumers step the current one.
+constexpr int kLifeThreads = (kLifeWarps + 1) * 32;  // 512
+constexpr int kLifeConsumerThreads = kLifeWarps * 32;
+// The TMA box: the window's 32 words start at word 30 tx - 1, which is not
+// 16-byte aligned; the box starts at the aligned word below it (x & ~3) and
+// is 36 words wide, and lanes read from the offset (0..3).
+constexpr int kLifeBoxWords = 36;
+constexpr uint32_t kLifeBoxBytes = kLifeWindowRows * kLifeBoxWords * 4;
+constexpr int kLifeBoxStride = (kLifeBoxBytes + 127) / 128 * 128;
+// Shared memory (bytes): source window, destination window (ring tiles), the
+// exchange rows (two parities x warps x {first, last} row x 32 lanes), M and D
+// of ring tiles (kLifeRows rows x 32 lanes per warp each), two mbarriers and
+// the item slot.
+constexpr int kLifeXchWords = 2 * kLifeWarps * 2 * 32;
+constexpr int kLifeRingWords = kLifeWarps * kLifeRows * 32;
+constexpr int kLifeSmemWords = 2 * kLifeBoxStride / 4 + kLifeXchWords + 2 * kLifeRingWords;
+constexpr size_t kLifeSmemBytes = static_cast<size_t>(kLifeSmemWords) * 4 + 64;
+static_assert(kLifeBoxBytes % 16 == 0, "TMA transaction bytes");
+
+struct LifeSlot {
+  int valid;  // 0: no more items (or an error): consumers leave
+  int pass, tile;
+};
+
+__device__ __forceinline__ void consumers_barrier() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kLifeConsumerThreads) : "memory");
+}
+
 // Every pass of a run in one launch. Work items (pass, tile) are handed out
-// in order by an atomic counter; before tile t of pass p is staged, thread 0
-// waits (bounded) until every tile of pass p-1 whose core the tile reads --
-// rows within ceil(T/TH) tiles, one tile column either side -- has completed
-// (done[] counts the passes each tile has completed). Those tiles also were
-// the last readers of the region this tile writes. All CTAs are resident and
-// items are taken in order, so every awaited item is held by a running CTA.
-// Planes written by other SMs are read through L2 (ld.global.cg).
-// Pass i has 1 + 2 * (q + (i < r)) steps (the odd-length plan of
-// plan_passes).
-__global__ void __launch_bounds__(kBThreads, 2)
-    life_bits_persistent_kernel(uint32_t* __restrict__ planeX, uint32_t* __restrict__ planeY, int PW, int W, int H,
-                                int ring, int npasses, int q, int r, int T, int TH, int LH, int tiles_x, int tiles_y,
+// in order by an atomic counter. The producer warp of a block takes an item,
+// waits (bounded) until every tile of pass p-1 whose core the item's window
+// reads -- rows within ceil(T/TH) tiles, one tile column either side -- has
+// completed (done[] counts the consumer warps that finished each tile, so a
+// pass is kLifeWarps counts), waits for the window buffer to be free and
+// loads the window (and, for ring tiles, the destination plane's) by TMA.
+// Those tiles were also the last readers of the region the item writes. All
+// blocks are resident and items are taken in order, so every awaited item is
+// held by a running block (possibly this one: its consumers finish the
+// current item without the producer). A latched error word stops the
+// producers at their next poll or item; the consumers then leave. Pass i has
+// 1 + 2 * (q + (i < r)) steps (the odd-length plan of plan_passes).
+__global__ void __launch_bounds__(kLifeThreads, 2)
+    life_bits_persistent_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant__ CUtensorMap mapY,
+                                uint32_t* __restrict__ planeX, uint32_t* __restrict__ planeY, int PW, int W, int H,
+                                int ring, int q, int r, int T, int TH, int tiles_x, int tiles_y,
                                 unsigned long long* next_item, unsigned* done, unsigned* err,
                                 const __grid_constant__ LifeWindow win) {
-  extern __shared__ __align__(128) uint32_t bsm[];
-  uint32_t* planeA = bsm;
-  uint32_t* planeB = bsm + kBPlane;
-  __shared__ long long s_item;
-  __shared__ int s_pass, s_tile;
-  (void)npasses;
+  extern __shared__ __align__(128) uint8_t lsm_raw[];
+  uint32_t* win_src = reinterpret_cast<uint32_t*>(lsm_raw);
+  uint32_t* win_dst = reinterpret_cast<uint32_t*>(lsm_raw + kLifeBoxStride);
+  uint32_t* xch = reinterpret_cast<uint32_t*>(lsm_raw + 2 * kLifeBoxStride);
+  uint32_t* Ms = xch + kLifeXchWords;
+  uint32_t* Ds = Ms + kLifeRingWords;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(lsm_raw + static_cast<size_t>(kLifeSmemWords) * 4);
+  uint64_t* full = &bars[0];
+  uint64_t* empty = &bars[1];
+  LifeSlot* slot = reinterpret_cast<LifeSlot*>(&bars[2]);
+  __shared__ int s_ok;
   const int tid = threadIdx.x;
-  for (int i = tid; i < 2 * kBPlane; i += kBThreads) bsm[i] = 0u;
+  const int lane = tid & 31, w = tid >> 5;
+  if ((smem_u32(lsm_raw) & 127u) != 0) {  // TMA needs the aligned base; uniform across the block
+    if (tid == 0) atomicOr(err, kDevErrAlign);
+    return;
+  }
+  if (tid == 0) {
+    mbar_init(full, 1);
+    mbar_init(empty, kLifeWarps);
+    fence_barrier_init();
+    prefetch_tensormap(&mapX);
+    prefetch_tensormap(&mapY);
+  }
   __syncthreads();
-  const int j = tid & (kBW - 1);
-  const int y0 = (tid / kBW) * kRowsPerStrip;
   const int ntiles = tiles_x * tiles_y;
   // this launch's items: passes win.pass0 .. + win.np, each over all tiles or
   // (windowed) over tile rows [win.lo[j], ...) holding win.start[j+1] -
   // win.start[j] items; completion counts persist between the launches of a run
   const long long nitems = win.windowed ? win.start[win.np] : static_cast<long long>(win.np) * ntiles;
-  const int dy = (T + TH - 1) / TH;
-  for (;;) {
-    if (tid == 0) {
-      const long long it = static_cast<long long>(atomicAdd(next_item, 1ull));
-      s_item = it;
-      if (it < nitems) {
+
+  if (w == kLifeWarps) {
+    // ---------------------------------------------------------- producer
+    if (lane != 0) return;
+    const int dy = (T + TH - 1) / TH;
+    uint32_t empty_phase = 0;
+    for (long long k = 0;; ++k) {
+      const long long it = error_latched(err) ? nitems : static_cast<long long>(atomicAdd(next_item, 1ull));
+      int valid = it < nitems ? 1 : 0;
+      int pass = 0, tile = 0;
+      if (valid) {
         if (win.windowed) {
           int j = 0;
           while (j + 1 < win.np && win.start[j + 1] <= it) ++j;
-          const long long k = it - win.start[j];
-          s_pass = win.pass0 + j;
-          s_tile = static_cast<int>((win.lo[j] + k / tiles_x) * tiles_x + k % tiles_x);
+          const long long kk = it - win.start[j];
+          pass = win.pass0 + j;
+          tile = static_cast<int>((win.lo[j] + kk / tiles_x) * tiles_x + kk % tiles_x);
         } else {
-          s_pass = win.pass0 + static_cast<int>(it / ntiles);
-          s_tile = static_cast<int>(it % ntiles);
+          pass = win.pass0 + static_cast<int>(it / ntiles);
+          tile = static_cast<int>(it % ntiles);
         }
       }
-    }
-    __syncthreads();
-    const long long item = s_item;
-    if (item >= nitems) break;
-    const int pass = s_pass;
-    const int tile = s_tile;
-    const int steps = 1 + 2 * (q + (pass < r ? 1 : 0));
-    const uint32_t* src = (pass & 1) ? planeY : planeX;
-    uint32_t* dst = (pass & 1) ? planeX : planeY;
-    const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
-    int ok = 1;
-    if (tid == 0 && pass > 0) {
-      for (int yy = max(0, ty - dy); yy <= min(tiles_y - 1, ty + dy) && ok; ++yy) {
-        for (int xx = max(0, tx - 1); xx <= min(tiles_x - 1, tx + 1) && ok; ++xx) {
-          const unsigned* d = &done[yy * tiles_x + xx];
-          unsigned polls = 0;
-          while (ld_acquire_u32(d) < static_cast<unsigned>(pass)) {
-            if (++polls >= kLifeSpinLimit) {
-              atomicOr(err, kDevErrBarrier);
-              ok = 0;
-              break;
+      const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+      if (valid && pass > 0) {
+        const unsigned need = static_cast<unsigned>(pass) * kLifeWarps;
+        for (int yy = max(0, ty - dy); yy <= min(tiles_y - 1, ty + dy) && valid; ++yy) {
+          for (int xx = max(0, tx - 1); xx <= min(tiles_x - 1, tx + 1) && valid; ++xx) {
+            const unsigned* d = &done[yy * tiles_x + xx];
+            unsigned polls = 0;
+            while (ld_acquire_u32(d) < need) {
+              if (error_latched(err)) {  // another block gave up: stop, it reported why
+                valid = 0;
+                break;
+              }
+              if (++polls >= kLifeSpinLimit) {
+                atomicOr(err, kDevErrBarrier);
+                valid = 0;
+                break;
+              }
+              __nanosleep(32);
             }
-            __nanosleep(32);
           }
         }
       }
+      // the consumers have copied the previous window (and read its slot)
+      if (k > 0) {
+        if (!mbar_wait_bounded(empty, empty_phase, err)) valid = 0;
+        empty_phase ^= 1u;
+      }
+      slot->valid = valid;
+      slot->pass = pass;
+      slot->tile = tile;
+      if (!valid) {
+        mbar_arrive(full);  // releases the consumers with valid = 0
+        return;
+      }
+      const int wy0 = ty * TH - T;
+      const int gx = tx * kLifeCoreWords - 1;
+      const bool ring_tile = wy0 < ring || wy0 + kLifeWindowRows > H - ring || gx * 32 < ring ||
+                             (gx + 32) * 32 > W - ring;
+      const CUtensorMap* msrc = (pass & 1) ? &mapY : &mapX;
+      const CUtensorMap* mdst = (pass & 1) ? &mapX : &mapY;
+      // the tiles awaited above wrote through the generic proxy; TMA reads
+      // through the async proxy
+      fence_proxy_async_global();
+      mbar_arrive_expect_tx(full, kLifeBoxBytes * (ring_tile ? 2u : 1u));
+      tma_load_2d(win_src, msrc, gx & ~3, wy0, full);
+      if (ring_tile) tma_load_2d(win_dst, mdst, gx & ~3, wy0, full);
     }
-    if (!__syncthreads_and(ok)) break;
-    __threadfence();
-    const int gy0 = ty * TH - T;
-    const int gw0 = tx * kBCore - 1;
-    const int gx0 = gw0 * 32;
-    const bool ring_tile = (gy0 < ring) || (gy0 + LH > H - ring) || (gx0 < ring) || (gx0 + kBW * 32 > W - ring);
-    const int nstage = ring_tile ? 2 : 1;
-    for (int k = 0; k < nstage; ++k) {
-      const uint32_t* g = (k == 0) ? src : dst;
-      uint32_t* pl = (k == 0) ? planeA : planeB;
-#pragma unroll 8
-      for (int i = tid; i < LH * kBW; i += kBThreads) {
-        const int row = i / kBW, wd = i - row * kBW;
-        const int gy = gy0 + row, gw = gw0 + wd;
-        const bool in = gy >= 0 && gy < H && gw >= 0 && gw < PW;
-        pl[(row + 1) * kBP + wd + 1] = in ? ld_cg(g + static_cast<int64_t>(gy) * PW + gw) : 0u;
+  }
+
+  // ------------------------------------------------------------ consumers
+  uint32_t* Mw = Ms + w * kLifeRows * 32;
+  uint32_t* Dw = Ds + w * kLifeRows * 32;
+  uint32_t full_phase = 0;
+  for (;;) {
+    // one thread waits (bounded) and the decision is shared, so every
+    // consumer warp takes the same path through the named barriers below
+    if (tid == 0) s_ok = mbar_wait_bounded(full, full_phase, err) ? 1 : 0;
+    consumers_barrier();
+    if (!s_ok) break;
+    mbar_try_wait(full, full_phase);  // completed: the TMA data is visible to this thread too
+    full_phase ^= 1u;
+    const volatile LifeSlot* vs = slot;
+    if (!vs->valid) break;
+    const int pass = vs->pass, tile = vs->tile;
+    const int steps = 1 + 2 * (q + (pass < r ? 1 : 0));
+    uint32_t* dst = (pass & 1) ? planeX : planeY;
+    const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    const int wy0 = ty * TH - T;
+    const int gx = tx * kLifeCoreWords - 1;
+    const int gw = gx + lane;
+    const int col = (gx - (gx & ~3)) + lane;  // this lane's word in the box
+    const int gyw = wy0 + w * kLifeRows;      // this warp's row 0
+    const bool ring_tile = wy0 < ring || wy0 + kLifeWindowRows > H - ring || gx * 32 < ring ||
+                           (gx + 32) * 32 > W - ring;
+    uint32_t x[kLifeRows + 2];
+#pragma unroll
+    for (int i = 0; i < kLifeRows + 2; ++i) x[i] = win_src[(w * kLifeRows + i) * kLifeBoxWords + col];
+    if (ring_tile) {
+      // interior mask and ring flip of the rows this warp steps (only it reads them)
+      const bool gw_in = gw >= 0 && gw < PW;
+      const uint32_t colmask = gw_in ? bit_range(ring - 32 * gw, (W - ring) - 32 * gw) : 0u;
+#pragma unroll
+      for (int i = 1; i <= kLifeRows; ++i) {
+        const int gy = gyw + i;
+        const uint32_t m = (gw_in && gy >= ring && gy < H - ring) ? colmask : 0u;
+        const uint32_t b = win_dst[(w * kLifeRows + i) * kLifeBoxWords + col];
+        Mw[(i - 1) * 32 + lane] = m;
+        Dw[(i - 1) * 32 + lane] = (x[i] ^ b) & ~m;
       }
     }
-    for (int i = LH * kBW + tid; i < kBRows * kBW; i += kBThreads) {
-      const int row = i / kBW, wd = i - row * kBW;
-      planeA[(row + 1) * kBP + wd + 1] = 0u;
-      planeB[(row + 1) * kBP + wd + 1] = 0u;
-    }
-    __syncthreads();
-    const uint32_t colmask = bit_range(ring - (gx0 + 32 * j), (W - ring) - (gx0 + 32 * j));
-    const bool active = y0 < LH;
+    __syncwarp();
+    if (lane == 0) mbar_arrive(empty);  // this warp is done with the window and the slot
+    int par = 0;
     for (int s = 0; s < steps; ++s) {
-      const uint32_t* in = (s & 1) ? planeB : planeA;
-      uint32_t* out = (s & 1) ? planeA : planeB;
-      if (active) {
-        if (ring_tile) {
-          life_strip<true, kBP>(in, out, y0, j, colmask, gy0, ring, H);
-        } else {
-          life_strip<false, kBP>(in, out, y0, j, colmask, gy0, ring, H);
-        }
+      if (ring_tile) {
+        life_reg_step<true>(x, Mw, Dw, lane);
+      } else {
+        life_reg_step<false>(x, Mw, Dw, lane);
       }
-      __syncthreads();
+      if (s + 1 < steps) {
+        // exchange the first and last rows with the warps above and below;
+        // two parities, so one barrier per step suffices (a slot is rewritten
+        // two steps later, after every warp has passed the barrier between)
+        uint32_t* xb = xch + par * (2 * kLifeWarps * 32);
+        xb[(2 * w) * 32 + lane] = x[1];
+        xb[(2 * w + 1) * 32 + lane] = x[kLifeRows];
+        consumers_barrier();
+        if (w > 0) x[0] = xb[(2 * (w - 1) + 1) * 32 + lane];
+        if (w < kLifeWarps - 1) x[kLifeRows + 1] = xb[(2 * (w + 1)) * 32 + lane];
+        par ^= 1;
+      }
     }
-    const uint32_t* fin = (steps & 1) ? planeB : planeA;
-    for (int i = tid; i < TH * kBCore; i += kBThreads) {
-      const int rr = i / kBCore, wd = 1 + (i - rr * kBCore);
-      const int row = T + rr;
-      const int gy = gy0 + row, gw = gw0 + wd;
-      if (gy < 0 || gy >= H || gw >= PW) continue;
-      dst[static_cast<int64_t>(gy) * PW + gw] = fin[(row + 1) * kBP + wd + 1];
+    // write back the core: rows [ty*TH, ty*TH + TH) of the grid, lanes 1..30
+    const int gc0 = ty * TH;
+    const int gc1 = min(H, gc0 + TH);
+    if (lane >= 1 && lane <= kLifeCoreWords && gw < PW) {
+#pragma unroll
+      for (int i = 1; i <= kLifeRows; ++i) {
+        const int gy = gyw + i;
+        if (gy >= gc0 && gy < gc1) dst[static_cast<int64_t>(gy) * PW + gw] = x[i];
+      }
     }
     __threadfence();
-    __syncthreads();
-    if (tid == 0) atomicAdd(&done[tile], 1u);
+    __syncwarp();
+    if (lane == 0) atomicAdd(&done[tile], 1u);
   }
 }
 
@@ -346,11 +460,13 @@ __global__ void __launch_bounds__(kBThreads, 2)
 
 int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
 
-int life_bits_tiles(int W, int H, int TH) {
-  return ((life_bits_words(W) + kBCore - 1) / kBCore) * ((H + TH - 1) / TH);
-}
+int life_bits_tiles_x(int W) { return (life_bits_words(W) + kLifeCoreWords - 1) / kLifeCoreWords; }
 
-size_t life_bits_smem_bytes() { return 2 * static_cast<size_t>(kBPlane) * sizeof(uint32_t); }
+int life_bits_max_tile_h(int T) { return kLifeWindowRows - 2 * T; }
+
+int life_bits_tiles(int W, int H, int TH) { return life_bits_tiles_x(W) * ((H + TH - 1) / TH); }
+
+size_t life_bits_smem_bytes() { return kLifeSmemBytes; }
 
 
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
@@ -391,27 +507,20 @@ int life_bits_persistent_ctas_per_sm() {
   const size_t smem = life_bits_smem_bytes();
   cudaFuncSetAttribute(life_bits_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        static_cast<int>(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_persistent_kernel, kBThreads, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_persistent_kernel, kLifeThreads, smem) !=
+      cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
 
 cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int ring, int npasses, int q, int r,
                                      int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s) {
-  const int LH = TH + 2 * T;
-  const int PW = life_bits_words(W);
-  const int tiles_x = (PW + kBCore - 1) / kBCore;
-  const int tiles_y = (H + TH - 1) / TH;
   cudaError_t e = cudaMemsetAsync(sync, 0, life_bits_sync_bytes(W, H, TH), s);
   if (e != cudaSuccess) return e;
-  unsigned long long* next = static_cast<unsigned long long*>(sync);
-  unsigned* done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
   LifeWindow win;
   memset(&win, 0, sizeof(win));
   win.np = npasses;
-  life_bits_persistent_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(
-      X, Y, PW, W, H, ring, npasses, q, r, T, TH, LH, tiles_x, tiles_y, next, done, err, win);
-  return cudaGetLastError();
+  return life_bits_run_window(X, Y, W, H, ring, win, q, r, T, TH, ctas, sync, err, s, false);
 }
 
 cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t s) {
@@ -419,18 +528,31 @@ cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t 
 }
 
 cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int ring, const LifeWindow& win, int q,
-                                 int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s) {
-  const int LH = TH + 2 * T;
+                                 int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s,
+                                 bool restart) {
+  if (T < 1 || T > kLifeBitsMaxT || TH < 1 || TH > life_bits_max_tile_h(T)) return cudaErrorInvalidValue;
   const int PW = life_bits_words(W);
-  const int tiles_x = (PW + kBCore - 1) / kBCore;
+  const int tiles_x = life_bits_tiles_x(W);
   const int tiles_y = (H + TH - 1) / TH;
   // the item counter restarts; the per-tile completion counts carry over
-  cudaError_t e = cudaMemsetAsync(sync, 0, 16, s);
-  if (e != cudaSuccess) return e;
+  if (restart) {
+    cudaError_t e = cudaMemsetAsync(sync, 0, 16, s);
+    if (e != cudaSuccess) return e;
+  }
   unsigned long long* next = static_cast<unsigned long long*>(sync);
   unsigned* done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
-  life_bits_persistent_kernel<<<ctas, kBThreads, life_bits_smem_bytes(), s>>>(
-      X, Y, PW, W, H, ring, win.pass0 + win.np, q, r, T, TH, LH, tiles_x, tiles_y, next, done, err, win);
+  // both planes as 2D tensors of 32-bit words (rows of PW words, 16-byte
+  // aligned: PW is a multiple of 4); boxes of 36 words x the window's rows,
+  // zero-filled outside the plane
+  CUtensorMap mx, my;
+  const uint64_t dims[2] = {static_cast<uint64_t>(PW), static_cast<uint64_t>(H)};
+  const uint64_t strides[1] = {static_cast<uint64_t>(PW) * 4};
+  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(kLifeWindowRows)};
+  cudaError_t e = encode_tmap(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, X, dims, strides, box);
+  if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
+  if (e != cudaSuccess) return e;
+  life_bits_persistent_kernel<<<ctas, kLifeThreads, life_bits_smem_bytes(), s>>>(
+      mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y, next, done, err, win);
   return cudaGetLastError();
 }
 

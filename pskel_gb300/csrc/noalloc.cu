@@ -84,14 +84,18 @@ extern "C" PSKEL_API pskel_status pskel_iterate3d_noalloc(const pskel_stencil* s
   if (pskel_status q = pskel::iterate3d(*st, in, out, width, height, depth, iterations, R, sched, residual_every,
                                         residuals, d->partials, kNoAllocPartials, &c, s))
     return q;
+  // the error word is read behind the run on the caller's stream, so only
+  // that stream is waited for (no legacy-stream copy that would wait for
+  // every other blocking stream of the device)
+  unsigned word = 0;
+  e = cudaMemcpyAsync(&word, d->err, sizeof(word), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return pskel::cuda_fail(e, "reading the device error word");
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return pskel::cuda_fail(e, "kernel execution");
-  unsigned word = 0;
-  e = cudaMemcpyFromSymbol(&word, g_noalloc_err, sizeof(word));
-  if (e != cudaSuccess) return pskel::cuda_fail(e, "reading the device error word");
   if (word) {
-    const unsigned zero = 0;
-    cudaMemcpyToSymbol(g_noalloc_err, &zero, sizeof(zero));
+    e = cudaMemsetAsync(d->err, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return pskel::cuda_fail(e, "clearing the device error word");
     return pskel::fail(PSKEL_ERR_DEVICE, "device error word 0x%x (a bounded wait timed out)", word);
   }
   return PSKEL_OK;

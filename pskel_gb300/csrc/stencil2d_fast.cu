@@ -16,6 +16,8 @@
 //
 // Arithmetic is the oracle's: products and sums in mask order with
 // __fmul_rn/__fadd_rn (no contraction), bf16 results rounded every step.
+#include <atomic>
+
 #include "fast2d_tile.cuh"
 
 namespace pskel {
@@ -142,9 +144,6 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* q) {
   return v;
 }
 
-__device__ __forceinline__ void fence_proxy_async_global() {
-  asm volatile("fence.proxy.async.global;" ::: "memory");
-}
 
 // Every pass of a run in one persistent launch (grids of few tiles per pass,
 // where the end of each pass would leave SMs idle and every launch adds its
@@ -154,6 +153,8 @@ __device__ __forceinline__ void fence_proxy_async_global() {
 // (done[] counts the passes each tile has completed). Those tiles are also
 // the last readers of t's core in the buffer pass i writes. An awaited item
 // precedes the waiting one, so a running CTA holds it or has finished it.
+// A wait that runs out latches kDevErrBarrier; the other CTAs see the latched
+// word at their next poll or item and stop.
 // Even passes read `in` (map_in) and write `out`, odd passes the reverse;
 // pass i has 1 + 2 * (q + (i < r)) steps (the odd-length plan).
 template <class TS, int OpK, int S>
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   const int dx = (p.HX + p.TW - 1) / p.TW;
   uint32_t phase_bits = 0;  // bit i: parity of the next completion of bars[i]
   for (;;) {
-    if (tid == 0) s_item = static_cast<long long>(atomicAdd(run.next_item, 1ull));
+    if (tid == 0) s_item = error_latched(p.err) ? nitems : static_cast<long long>(atomicAdd(run.next_item, 1ull));
     __syncthreads();
     const long long item = s_item;
     if (item >= nitems) break;
@@ -216,6 +217,10 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
             const unsigned* d = &run.done[yy * p.tiles_x + xx];
             unsigned polls = 0;
             while (ld_acquire_gpu(d) < static_cast<unsigned>(pass)) {
+              if (error_latched(p.err)) {  // another CTA gave up and reported why
+                ok = 0;
+                break;
+              }
               if (++polls >= kFastSpinLimit) {
                 atomicOr(p.err, kDevErrBarrier);
                 ok = 0;
@@ -271,6 +276,27 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   }
 }
 
+// CTAs of `kern` that fit on the current device at once; cached per device
+// in `cache` (one array per kernel instantiation; threads that race both
+// compute the same value).
+constexpr int kMaxCachedDevices = 64;
+template <class Kern>
+int resident_ctas(Kern kern, size_t smem, std::atomic<int>* cache) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const bool cached = dev >= 0 && dev < kMaxCachedDevices;
+  if (cached) {
+    const int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+  }
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastThreads, smem);
+  const int v = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  if (cached) cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
 template <class TS, int OpK, int S>
 cudaError_t launch_multipass(const CUtensorMap* mi, const CUtensorMap* mo, const Stencil2DParams& p,
                              const Fast2DRun& run, int ctas, cudaStream_t s) {
@@ -280,14 +306,8 @@ cudaError_t launch_multipass(const CUtensorMap* mi, const CUtensorMap* mo, const
   if (e != cudaSuccess) return e;
   // every CTA resident (items are taken only by running CTAs, so this is for
   // speed, not for progress)
-  static int resident = 0;
-  if (resident == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastThreads, smem);
-    resident = (per_sm > 0 ? per_sm : 1) * sms;
-  }
+  static std::atomic<int> resident_by_device[kMaxCachedDevices];
+  const int resident = resident_ctas(kern, smem, resident_by_device);
   if (ctas > resident) ctas = resident;
   kern<<<ctas, kFastThreads, smem, s>>>(*mi, *mo, p, run);
   return cudaGetLastError();
@@ -312,14 +332,8 @@ cudaError_t launch_fast(const CUtensorMap* ms, const CUtensorMap* md, const CUte
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   // persistent CTAs: no more than can be resident (registers or shared memory)
-  static int resident = 0;
-  if (resident == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastThreads, smem);
-    resident = (per_sm > 0 ? per_sm : 1) * sms;
-  }
+  static std::atomic<int> resident_by_device[kMaxCachedDevices];
+  const int resident = resident_ctas(kern, smem, resident_by_device);
   if (ctas > resident) ctas = resident;
   kern<<<ctas, kFastThreads, smem, s>>>(*ms, *md, *mu, *mv, p);
   return cudaGetLastError();

@@ -362,9 +362,6 @@ struct S3Rows {
   static constexpr size_t kSmem = kSlots * static_cast<size_t>(kS3PlaneBytes) + 16 * kSlots;
 };
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 
 // barrier among the consumer warps only (the producer warp may have left)
 template <int kCons>

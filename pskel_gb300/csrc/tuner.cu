@@ -71,10 +71,11 @@ TileEstimate estimate_tiles(const pskel_stencil& st, int64_t W, int64_t H, int64
   };
   if (st.op == PSKEL_OP_LIFE) {
     g.T = clamp_odd(s.time_steps > 0 ? s.time_steps : 15, kLifeBitsMaxT);
-    g.TH = std::max(2, (s.tile_h > 0 ? std::min(s.tile_h, 256 - 2 * g.T) : 256 - 2 * g.T) & ~1);
+    const int th_max = life_bits_max_tile_h(g.T);
+    g.TH = std::max(1, s.tile_h > 0 ? std::min(s.tile_h, th_max) : th_max);
     g.LH = g.TH + 2 * g.T;
-    g.TW = 448;  // 14 core words of the 16-word bit-plane tile
-    g.LW = 512;
+    g.TW = 32 * kLifeCoreWords;  // the core words of a one-warp-wide bit-plane tile
+    g.LW = 32 * (kLifeCoreWords + 2);
     g.tall = false;
   } else if (fast_path(st)) {
     const int vec = st.dtype == PSKEL_BF16 ? 8 : 4;

@@ -163,6 +163,14 @@ int main(int argc, char** argv) {
     } else if (sc == "jacobi_user") {
       Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
       st.runIterativeGPU(it, 0, 0);
+    } else if (sc == "jacobi_user_tiling") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
+      st.runIterativeTilingGPU(it, 64, 24, 1, 5);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
+    } else if (sc == "jacobi_user_auto") {
+      Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
+      st.runIterativeAutoGPU(it);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
     } else if (sc == "jacobi_cpu") {
       Stencil2D<Array2D<float>, Mask2D<float>, JacobiUser> st(in, out, mask, JacobiUser{0});
       st.runIterativeCPU(it, 4);
@@ -201,12 +209,16 @@ int main(int argc, char** argv) {
         args.coef(static_cast<int>(w), static_cast<int>(h)) = 0.05f + 0.2f * static_cast<float>((h * 7 + w * 3) % 11) / 10.0f;
     Mask2D<float> mask = jacobi_mask();
     Stencil2D<Array2D<float>, Mask2D<float>, CoefArgs> st(in, out, mask, args);
-    if (sc == "coef_gpu")
+    if (sc == "coef_gpu") {
       st.runIterativeGPU(it, 0, 0);
-    else if (sc == "coef_cpu")
+    } else if (sc == "coef_tiling") {
+      st.runIterativeTilingGPU(it, 64, 16, 1, 3);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
+    } else if (sc == "coef_cpu") {
       st.runIterativeCPU(it, 4);
-    else
+    } else {
       return 3;
+    }
     write_raw(fres, out.hostArray, W * H);
   } else if (sc.rfind("stencil1d", 0) == 0) {
     // 1D: W cells; mask offsets -2, -1, 0, 1, 3 with halo value 0.5
@@ -269,6 +281,10 @@ int main(int argc, char** argv) {
     } else if (sc == "heat_user") {
       Stencil3D<Array3D<float>, Mask3D<float>, HeatUser> st(in, out, mask, HeatUser{0});
       st.runIterativeGPU(it, 0, 0);
+    } else if (sc == "heat_user_tiling") {
+      Stencil3D<Array3D<float>, Mask3D<float>, HeatUser> st(in, out, mask, HeatUser{0});
+      st.runIterativeTilingGPU(it, W, 6, D, 3);
+      if (st.ranOutOfCore()) std::printf("out of core\n");
     } else {
       return 3;
     }

@@ -25,3 +25,18 @@ def test_reference_arm_line():
     assert "whole workload" in cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": "GCells/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_maps_no_library_of_ours():
+    """The reference arm times only the reference: its process must not map
+    libpskel_gb300.so (the seeded generators import without opening it)."""
+    code = (
+        "import argparse, bench\n"
+        "a = argparse.Namespace(steps=1, warmup=1)\n"
+        "line = bench.run_reference_arm(a, dict(bench.WORKLOADS['jacobi'], name='jacobi'), 1, 0)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('MAPPED' if 'libpskel_gb300' in maps else 'CLEAN', line['value'] > 0)\n"
+    )
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.split() == ["CLEAN", "True"], r.stdout

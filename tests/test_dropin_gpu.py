@@ -147,6 +147,9 @@ def test_dropin_map(app, scenario, iters):
     ("jacobi_auto", (700, 520), 2 << 20),     # slabs sized from the budget
     ("life_tiling", (227, 301), 100_000),
     ("heat_tiling", (29, 37, 48), 300_000),   # slabs of 8 h-planes, 3 steps per visit
+    ("jacobi_user_tiling", (157, 203), 200_000),  # a user functor: slabs of 24 rows, 5 steps per visit
+    ("jacobi_user_auto", (700, 520), 2 << 20),    # a user functor, slabs sized from the budget
+    ("heat_user_tiling", (29, 37, 48), 300_000),  # a 3D user functor: slabs of 6 h-planes, 3 steps per visit
 ])
 @pytest.mark.parametrize("iters", [1, 6, 13])
 def test_dropin_out_of_core(app, oracle_mod, scenario, shape, budget, iters):
@@ -232,4 +235,20 @@ def test_dropin_args_field(app, scenario, iters):
     a = rng.uniform(0, 1, (97, 131)).astype(np.float32)
     b = rng.uniform(0, 1, (97, 131)).astype(np.float32)
     got, _ = run_app(app, scenario, a, b, iters)
+    assert np.array_equal(got.view(np.uint32), coef_run(a, b, iters).view(np.uint32))
+
+
+@pytest.mark.parametrize("iters", [1, 4, 9])
+def test_dropin_args_field_out_of_core(app, iters):
+    """The same functor out of core (slabs of 16 rows, 3 steps per visit):
+    it must see grid coordinates, so the field is read at the right cells."""
+    import os
+    rng = np.random.default_rng(iters + 50)
+    a = rng.uniform(0, 1, (97, 131)).astype(np.float32)
+    b = rng.uniform(0, 1, (97, 131)).astype(np.float32)
+    env = dict(os.environ, PSKEL_DEVICE_BYTES="60000")
+    assert 2 * a.nbytes > 60000
+    out = []
+    got, _ = run_app(app, "coef_tiling", a, b, iters, env=env, stdout=out)
+    assert "out of core" in out[0]
     assert np.array_equal(got.view(np.uint32), coef_run(a, b, iters).view(np.uint32))

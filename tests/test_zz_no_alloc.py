@@ -57,6 +57,44 @@ def test_noalloc_matches_regular_entry_point_twice(cuda):
         assert got_res.shape[0] == iters // every
 
 
+def test_noalloc_default_streaming_path_allocates_nothing(cuda):
+    """The schedule callers get by default: the one-step TMA streaming kernel
+    (7-point cross) with a residual every 10 steps, 50 steps on 64^3. Two
+    calls in a row match the regular entry point; once both entry points have
+    run (the first no-allocation call on a device looks up its arrays'
+    addresses, and the kernels load on first use), further calls leave the
+    device's free memory unchanged."""
+    torch = cuda
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, "f32", S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, keep=keep)
+    default = P.Schedule(time_steps=0, tile_w=0, tile_h=0, tile_d=0, ctas=0)
+    iters, every = 50, 10
+    shape = (64, 64, 64)
+    H, W, D = shape
+    res = torch.zeros(iters // every, dtype=torch.float64, device="cuda")
+
+    def noalloc(x, y):
+        rc = P.lib.pskel_iterate3d_noalloc(C.byref(st), x.data_ptr(), y.data_ptr(), W, H, D, iters, None, every,
+                                           res.data_ptr(), None)
+        assert rc == P.PSKEL_OK, P.lib.pskel_last_error().decode()
+
+    for call, seed in enumerate((11, 12)):
+        x0, y0 = _case(torch, seed, shape)
+        x, y = x0.clone(), y0.clone()
+        noalloc(x, y)
+        got, got_res = (y if iters % 2 else x).clone(), res.clone()
+        want, want_res = _call(P.lib.pskel_iterate3d, torch, st, x0.clone(), y0.clone(), iters, every, default)
+        assert torch.equal(got, want), f"call {call}: grids differ"
+        np.testing.assert_allclose(got_res.cpu().numpy(), want_res.cpu().numpy(), rtol=1e-12, atol=0)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        noalloc(x, y)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, f"free device memory changed across calls: {free_before} -> {free_after}"
+
+
 def test_noalloc_rejects_scratch_beyond_its_capacity(cuda):
     torch = cuda
     keep = P._Keep()

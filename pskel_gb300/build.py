@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "libpskel_gb300.so"
 
-SOURCES = ["capi.cu", "life.cu", "stencil2d.cu", "stencil2d_fast.cu", "stream2d.cu", "stencil3d.cu", "noalloc.cu", "batch.cu", "mlp.cu", "tuner.cu", "selftest.cu", "outofcore.cu"]
+SOURCES = ["capi.cu", "life.cu", "stencil2d.cu", "stencil2d_fast.cu", "stream2d.cu", "stencil3d.cu", "stream3d_tb.cu", "noalloc.cu", "batch.cu", "mlp.cu", "tuner.cu", "selftest.cu", "outofcore.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas",
               "-warn-spills", "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}"]

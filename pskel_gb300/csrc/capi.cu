@@ -617,61 +617,119 @@ pskel_status validate3d(const pskel_stencil* st, const void* in, const void* out
   return PSKEL_OK;
 }
 
+// The streaming 7-point kernels apply: the mask is the 7-point cross, D fills
+// whole 16-byte vectors, the buffers are 16-byte aligned, and (bf16) the halo
+// value is a bf16 value (the kernels hold halos in storage format).
+static bool cross7_ok(const pskel_stencil& st, const void* in, const void* out, int64_t D) {
+  const size_t esz = dtype_size(st.dtype);
+  uint32_t hb;
+  std::memcpy(&hb, &st.mask.halo_value, sizeof(hb));
+  const bool halo_exact = st.dtype != PSKEL_BF16 || (hb & 0xFFFFu) == 0u;
+  return stream3d_is_cross7(st.mask.offsets, st.mask.size, D, static_cast<int>(esz)) && halo_exact &&
+         (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0;
+}
+
+// Steps per pass of the 7-point cross by default: two (one HBM round trip per
+// two steps; measured on GB300).
+constexpr int kCross7DefaultSteps = 2;
+
+// Per-pass lengths of a two-step run: an even number of two-step passes and
+// the rest one-step passes, so that the pass count has the parity of `iters`
+// and the state ends in the buffer the step-by-step ping-pong ends in.
+static std::vector<int> plan_tb2(int64_t iters) {
+  std::vector<int> p;
+  const int64_t twos = (iters / 2) & ~int64_t(1);
+  for (int64_t i = 0; i < twos; ++i) p.push_back(2);
+  for (int64_t i = 0; i < iters - 2 * twos; ++i) p.push_back(1);
+  return p;
+}
+
 // The 7-point cross, one step per launch, planes staged by TMA: persistent
 // blocks over work items of (32 vectors of d) x 16 w x HC planes, about four
 // items per resident block.
 static pskel_status stream3d_cross7(const pskel_stencil& st, Stencil3DParams& p, void* in, void* out, int64_t W,
                                     int64_t H, int64_t D, int64_t iters, const pskel_schedule* sched, int64_t every,
                                     double* partials_override, int64_t partials_cap, DeviceContext* c,
-                                    cudaStream_t s) {
+                                    cudaStream_t s, int steps) {
   const int dtype = static_cast<int>(st.dtype);
   const int esz = static_cast<int>(dtype_size(st.dtype));
-  const int per_sm = stream3d_tma_blocks_per_sm(dtype);
-  const int64_t resident = static_cast<int64_t>(per_sm) * c->sms;
+  const std::vector<int> passes = steps == 2 ? plan_tb2(iters) : std::vector<int>(static_cast<size_t>(iters), 1);
+  const bool any2 = !passes.empty() && passes.front() == 2;
+  const bool any1 = !passes.empty() && passes.back() == 1;
   const int64_t cols = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), 1, esz);
-  int64_t chunks = std::max<int64_t>(1, (4 * resident + cols - 1) / cols);
-  chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / 8));
-  if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
-  p.HC = static_cast<int>((H + chunks - 1) / chunks);
-  p.hchunks = static_cast<int>((H + p.HC - 1) / p.HC);
-  const int64_t items = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), p.hchunks, esz);
-  int64_t ctas = std::min<int64_t>(items, resident);
-  if (sched && sched->ctas > 0) ctas = std::min<int64_t>(ctas, sched->ctas);
+  // h chunks: `per_block` items per resident block (the two-step kernel
+  // re-reads two planes more per item, so its items are longer), each of at
+  // least `min_planes` planes, or tile_h planes
+  auto configure = [&](Stencil3DParams& q, int per_sm, int per_block, int64_t min_planes, int64_t& ctas) {
+    const int64_t resident = static_cast<int64_t>(per_sm) * c->sms;
+    int64_t chunks = std::max<int64_t>(1, (per_block * resident + cols - 1) / cols);
+    chunks = std::min<int64_t>(chunks, std::max<int64_t>(1, H / min_planes));
+    if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
+    q.HC = static_cast<int>((H + chunks - 1) / chunks);
+    q.hchunks = static_cast<int>((H + q.HC - 1) / q.HC);
+    const int64_t items = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), q.hchunks, esz);
+    ctas = std::min<int64_t>(items, resident);
+    if (sched && sched->ctas > 0) ctas = std::min<int64_t>(ctas, sched->ctas);
+  };
+  Stencil3DParams p2 = p;
+  int64_t ctas1 = 0, ctas2 = 0;
+  configure(p, stream3d_tma_blocks_per_sm(dtype), 4, 8, ctas1);
+  if (any2) configure(p2, stream3d_tb2_blocks_per_sm(dtype), 2, 16, ctas2);
   if (every > 0) {
+    const int64_t need = std::max<int64_t>(any1 ? ctas1 : 0, any2 ? 2 * ctas2 : 0);
+    double* part = nullptr;
     if (partials_override) {
-      if (ctas > partials_cap)
+      if (need > partials_cap)
         return fail(PSKEL_ERR_UNSUPPORTED, "residual scratch of %lld partials exceeds the fixed capacity %lld",
-                    (long long)ctas, (long long)partials_cap);
-      p.partials = partials_override;
+                    (long long)need, (long long)partials_cap);
+      part = partials_override;
     } else {
-      if (pskel_status q = ensure_buffer(c->partials, static_cast<size_t>(ctas) * sizeof(double))) return q;
-      p.partials = static_cast<double*>(c->partials.ptr);
+      if (pskel_status q = ensure_buffer(c->partials, static_cast<size_t>(need) * sizeof(double))) return q;
+      part = static_cast<double*>(c->partials.ptr);
     }
+    p.partials = p2.partials = part;
   }
-  // the grid as 32-bit words: a 16-byte vector is 4 words for either dtype
-  CUtensorMap maps[2];
+  // the grid as 32-bit words: a 16-byte vector is 4 words for either dtype;
+  // boxes of 136 words x (16 rows + the halo rows of the kernel) x 1 plane
+  CUtensorMap maps1[2], maps2[2];
   const uint64_t dims[3] = {static_cast<uint64_t>(D) * esz / 4, static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
   const uint64_t strides[2] = {static_cast<uint64_t>(D) * esz, static_cast<uint64_t>(D) * esz * W};
-  const uint32_t box[3] = {136, 18, 1};
-  cudaError_t e = encode_tmap(&maps[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, in, dims, strides, box);
-  if (e == cudaSuccess) e = encode_tmap(&maps[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, out, dims, strides, box);
+  const uint32_t box1[3] = {136, 18, 1};
+  const uint32_t box2[3] = {136, stream3d_tb2_box_rows(), 1};
+  cudaError_t e = cudaSuccess;
+  if (any1) {
+    e = encode_tmap(&maps1[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, in, dims, strides, box1);
+    if (e == cudaSuccess) e = encode_tmap(&maps1[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, out, dims, strides, box1);
+  }
+  if (any2 && e == cudaSuccess) {
+    e = encode_tmap(&maps2[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, in, dims, strides, box2);
+    if (e == cudaSuccess) e = encode_tmap(&maps2[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, out, dims, strides, box2);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled (3D planes)");
-  for (int64_t k = 0; k < iters; ++k) {
-    const bool fwd = (k % 2 == 0);
-    p.src = fwd ? in : out;
-    p.dst = fwd ? out : in;
-    p.steps = 1;
-    p.step0 = k;
-    e = stream3d_tma_step(dtype, &maps[fwd ? 0 : 1], p, static_cast<int>(ctas), s);
+  int64_t k = 0;
+  for (size_t i = 0; i < passes.size(); ++i) {
+    const bool fwd = (i % 2 == 0);
+    Stencil3DParams& q = passes[i] == 2 ? p2 : p;
+    q.src = fwd ? in : out;
+    q.dst = fwd ? out : in;
+    q.steps = passes[i];
+    q.step0 = k;
+    if (passes[i] == 2)
+      e = stream3d_tb2_pass(dtype, &maps2[fwd ? 0 : 1], q, static_cast<int>(ctas2), s);
+    else
+      e = stream3d_tma_step(dtype, &maps1[fwd ? 0 : 1], q, static_cast<int>(ctas1), s);
     if (e != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
+    k += passes[i];
   }
   return PSKEL_OK;
 }
 
 // One step per launch with the streaming kernel (no temporal blocking).
+// steps: 1, or 2 for the two-step 7-point kernel (the 7-point cross only).
 static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t D,
                              int64_t iters, int R, const pskel_schedule* sched, int64_t every, double* residuals,
-                             double* partials_override, int64_t partials_cap, DeviceContext* c, cudaStream_t s) {
+                             double* partials_override, int64_t partials_cap, DeviceContext* c, cudaStream_t s,
+                             int steps = 1) {
   Stencil3DParams p;
   memset(&p, 0, sizeof(p));
   p.W = static_cast<int>(W);
@@ -689,15 +747,8 @@ static pskel_status stream3d(const pskel_stencil& st, void* in, void* out, int64
   p.err = c->err;
   p.every = static_cast<int>(every);
   p.residuals = residuals;
-  const size_t esz = dtype_size(st.dtype);
-  // the staged kernel holds halo values in storage format: a bf16 grid needs
-  // a halo value that bf16 represents exactly
-  uint32_t hb;
-  std::memcpy(&hb, &st.mask.halo_value, sizeof(hb));
-  const bool halo_exact = st.dtype != PSKEL_BF16 || (hb & 0xFFFFu) == 0u;
-  const bool cross7 = stream3d_is_cross7(st.mask.offsets, st.mask.size, D, static_cast<int>(esz)) && halo_exact &&
-                      (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0;
-  if (cross7) return stream3d_cross7(st, p, in, out, W, H, D, iters, sched, every, partials_override, partials_cap, c, s);
+  if (cross7_ok(st, in, out, D))
+    return stream3d_cross7(st, p, in, out, W, H, D, iters, sched, every, partials_override, partials_cap, c, s, steps);
   // h chunks: a few blocks per SM slot, each marching at least 16 planes
   const int64_t cols = stream3d_ctas(static_cast<int>(W), static_cast<int>(D), 1);
   int64_t chunks = std::max<int64_t>(1, (static_cast<int64_t>(32) * c->sms + cols - 1) / cols);
@@ -735,11 +786,13 @@ pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, 
   const int dtype = static_cast<int>(st.dtype);
   const size_t esz = dtype_size(st.dtype);
   const int vec = static_cast<int>(16 / esz);
-  int T = (sched && sched->time_steps > 0) ? sched->time_steps : 1;
+  const bool cross7 = cross7_ok(st, in, out, D);
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : (cross7 ? kCross7DefaultSteps : 1);
   T = static_cast<int>(std::min<int64_t>(std::min(T, kMax3DSteps), std::max<int64_t>(iters, 1)));
   if (R == 0) T = 1;
-  if (T == 1) return stream3d(st, in, out, W, H, D, iters, R, sched, every, residuals, partials_override,
-                              partials_cap, c, s);
+  if (T == 1 || (T == 2 && cross7))
+    return stream3d(st, in, out, W, H, D, iters, R, sched, every, residuals, partials_override, partials_cap, c, s,
+                    T);
   int TW = (sched && sched->tile_w > 0) ? sched->tile_w : 32;
   int TD = (sched && sched->tile_d > 0) ? sched->tile_d : 64;
   TD = std::max(vec, (TD / vec) * vec);

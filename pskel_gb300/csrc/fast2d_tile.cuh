@@ -62,6 +62,25 @@ __host__ __device__ constexpr Shape<K> shape_of() {
 
 constexpr int kFastThreads = 512;
 constexpr int kFastBufs = 3;  // rotating tile buffers: source, partner, next source
+constexpr int kFastWarps = kFastThreads / 32;
+
+// Warp w of the tile routine and warp w+1 share named barrier 1 + w (ids
+// 1..15; 0 is the block barrier). Between two steps a warp meets its two
+// neighbours only -- the warps whose rows it reads and who read its rows --
+// in two rounds: even warps first with the warp below, odd warps first with
+// the warp above, so pairs (0,1), (2,3), ... meet first and (1,2), (3,4), ...
+// second, and no chain of waits runs through the block.
+static_assert(kFastWarps <= 16, "one named barrier per neighbouring pair, ids 1..15");
+__device__ __forceinline__ void pair_barrier(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void neighbours_barrier(int w) {
+  if ((w & 1) == 0) {
+    if (w + 1 < kFastWarps) pair_barrier(1 + w);
+    if (w > 0) pair_barrier(w);
+  } else {
+    pair_barrier(w);
+    if (w + 1 < kFastWarps) pair_barrier(1 + w);
+  }
+}
 
 // Wind vector at (gy, gx..gx+3) straight from global memory (read-only path;
 // the tile's winds stay in L1 across the steps of a pass). Zero outside the grid.
@@ -145,7 +164,7 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
     // ring cell there keeps the buffer's value as a computed one would. The
     // test is uniform per warp; a warp with no such row skips the step.
     if (yb + S <= s || yb >= LH - s) {
-      __syncthreads();
+      neighbours_barrier(warp);
       continue;
     }
     // window: rows yb-1 .. yb+S, each [left, v0..v3, right]; the left and
@@ -194,8 +213,11 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
       }
       st_vec(o, res);
     }
-    __syncthreads();
+    // a step's rows are read by the warps above and below at the next step,
+    // and overwritten one step later only after they have met again
+    neighbours_barrier(warp);
   }
+  __syncthreads();  // the write-back reads every warp's rows
 
   // core -> global, interior cells only, vector stores
   const TS* fin = ((g.steps & 1) ? pbuf : sbuf);

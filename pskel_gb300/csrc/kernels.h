@@ -197,6 +197,21 @@ struct Stencil3DParams {
   int hbeg, hend;      // streaming 7-point kernel: planes [hbeg, hend) (hend 0: all)
 };
 
+// The 7-point cross, two steps per launch (stream3d_tb.cu): the one-step
+// streaming kernel's items with the second step fused behind the first in
+// shared memory. Reads p.src (through `map`: the grid as 32-bit words, boxes
+// of 136 words x stream3d_tb2_box_rows() rows x 1 plane), writes the state
+// after two steps to p.dst. Residual partials: 2 x ctas doubles when a step of
+// the pass is reported; the norms are reduced into p.residuals.
+int stream3d_tb2_blocks_per_sm(int dtype);
+uint32_t stream3d_tb2_box_rows();
+cudaError_t stream3d_tb2_pass(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas,
+                              cudaStream_t s);
+// Sums `steps` levels of per-CTA partials (level k at (k-1) * ctas) in a fixed
+// order and stores sqrt at residuals[(step0 + k) / every - 1] for reported k.
+cudaError_t stream3d_reduce_residuals(const double* partials, int ctas, int steps, int64_t step0, int every,
+                                      double* residuals, cudaStream_t s);
+
 size_t stencil3d_smem_bytes(int LW, int LD, int NP, int T, size_t esize);
 int stencil3d_max_ctas_per_sm(size_t smem);
 // One step of the generic streaming (not temporally blocked) kernel: a block

@@ -31,6 +31,8 @@
 // refreshed) and at lanes 0 and 31 (no neighbour lane) and advances one cell
 // per step, so after T <= 31 steps rows T .. T + TH - 1 of the window and
 // lanes 1..30 are exact.
+#include <cstdlib>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -107,14 +109,14 @@ __device__ __forceinline__ void row_sums(uint32_t c, uint32_t& t0, uint32_t& t1,
 // (s0 | alive): count 3, or count 2 and alive. A count of 8 leaves y1 set,
 // so it is dead as it must be. kRing: cells outside the interior mask M of
 // the row take old ^ D instead (M, D per row and lane in shared memory).
-template <bool kRing>
-__device__ __forceinline__ void life_reg_step(uint32_t (&x)[kLifeRows + 2], const uint32_t* __restrict__ Mw,
+template <bool kRing, int R>
+__device__ __forceinline__ void life_reg_step(uint32_t (&x)[R + 2], const uint32_t* __restrict__ Mw,
                                               const uint32_t* __restrict__ Dw, int lane) {
   uint32_t a0, a1, u0, u1, b0, b1, q0, q1;
   row_sums(x[0], a0, a1, u0, u1);
   row_sums(x[1], b0, b1, q0, q1);
 #pragma unroll
-  for (int i = 1; i <= kLifeRows; ++i) {
+  for (int i = 1; i <= R; ++i) {
     uint32_t c0, c1, r0, r1;
     row_sums(x[i + 1], c0, c1, r0, r1);  // row i+1 still holds the previous step
     const uint32_t s0 = lop3<kXor3>(a0, q0, c0);
@@ -226,35 +228,60 @@ __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) {
   return v;
 }
 
-// A block is kLifeWarps consumer warps, which hold and step the tile, and one
-// producer warp, which fetches the next work item, waits for its
-// dependencies and loads its window by TMA into shared memory while the
+// A block is NW consumer warps, which hold and step the tile (R rows per
+// lane), and one producer warp, which fetches the next work item, waits for
+// its dependencies and loads its window by TMA into shared memory while the
 // consumers step the current one.
-constexpr int kLifeThreads = (kLifeWarps + 1) * 32;  // 512
-constexpr int kLifeConsumerThreads = kLifeWarps * 32;
 // The TMA box: the window's 32 words start at word 30 tx - 1, which is not
 // 16-byte aligned; the box starts at the aligned word below it (x & ~3) and
 // is 36 words wide, and lanes read from the offset (0..3).
 constexpr int kLifeBoxWords = 36;
-constexpr uint32_t kLifeBoxBytes = kLifeWindowRows * kLifeBoxWords * 4;
-constexpr int kLifeBoxStride = (kLifeBoxBytes + 127) / 128 * 128;
-// Shared memory (bytes): source window, destination window (ring tiles), the
-// exchange rows (two parities x warps x {first, last} row x 32 lanes), M and D
-// of ring tiles (kLifeRows rows x 32 lanes per warp each), two mbarriers and
-// the item slot.
-constexpr int kLifeXchWords = 2 * kLifeWarps * 2 * 32;
-constexpr int kLifeRingWords = kLifeWarps * kLifeRows * 32;
-constexpr int kLifeSmemWords = 2 * kLifeBoxStride / 4 + kLifeXchWords + 2 * kLifeRingWords;
-constexpr size_t kLifeSmemBytes = static_cast<size_t>(kLifeSmemWords) * 4 + 64;
-static_assert(kLifeBoxBytes % 16 == 0, "TMA transaction bytes");
+template <int R, int NW>
+struct LifeGeo {
+  static constexpr int kWindowRows = NW * R + 2;
+  static constexpr int kThreads = (NW + 1) * 32;
+  static constexpr int kConsumerThreads = NW * 32;
+  static constexpr uint32_t kBoxBytes = kWindowRows * kLifeBoxWords * 4;
+  static constexpr int kBoxStride = (kBoxBytes + 127) / 128 * 128;
+  // shared memory (bytes): source window, destination window (ring tiles),
+  // the exchange rows (two parities x warps x {first, last} row x 32 lanes),
+  // M and D of ring tiles (R rows x 32 lanes per warp each), two mbarriers
+  // and the item slot
+  static constexpr int kXchWords = 2 * NW * 2 * 32;
+  static constexpr int kRingWords = NW * R * 32;
+  static constexpr int kSmemWords = 2 * kBoxStride / 4 + kXchWords + 2 * kRingWords;
+  static constexpr size_t kSmemBytes = static_cast<size_t>(kSmemWords) * 4 + 64;
+  static_assert(kBoxBytes % 16 == 0, "TMA transaction bytes");
+  static_assert(kWindowRows <= 256, "TMA box rows");
+  static_assert(NW <= 15, "one named barrier per neighbouring pair, ids 1..14, and 15 for all consumers");
+};
 
 struct LifeSlot {
   int valid;  // 0: no more items (or an error): consumers leave
   int pass, tile;
 };
 
+// All consumer warps (named barrier 15; the producer warp takes no part).
+template <int NW>
 __device__ __forceinline__ void consumers_barrier() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kLifeConsumerThreads) : "memory");
+  asm volatile("bar.sync 15, %0;" ::"n"(NW * 32) : "memory");
+}
+
+// Consumer warp w and w+1 share named barrier 1 + w (ids 1..14). A warp
+// synchronises with its two neighbours only, in two rounds -- even warps
+// first with the warp below, odd warps first with the warp above -- so the
+// pairs (0,1), (2,3), ... meet first and (1,2), (3,4), ... second, and no
+// chain of waits runs through the block.
+__device__ __forceinline__ void pair_barrier(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+template <int NW>
+__device__ __forceinline__ void neighbours_barrier(int w) {
+  if ((w & 1) == 0) {
+    if (w + 1 < NW) pair_barrier(1 + w);
+    if (w > 0) pair_barrier(w);
+  } else {
+    pair_barrier(w);
+    if (w + 1 < NW) pair_barrier(1 + w);
+  }
 }
 
 // Every pass of a run in one launch. Work items (pass, tile) are handed out
@@ -270,19 +297,21 @@ __device__ __forceinline__ void consumers_barrier() {
 // current item without the producer). A latched error word stops the
 // producers at their next poll or item; the consumers then leave. Pass i has
 // 1 + 2 * (q + (i < r)) steps (the odd-length plan of plan_passes).
-__global__ void __launch_bounds__(kLifeThreads, 2)
+template <int R, int NW, int kMinBlocks>
+__global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
     life_bits_persistent_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant__ CUtensorMap mapY,
                                 uint32_t* __restrict__ planeX, uint32_t* __restrict__ planeY, int PW, int W, int H,
                                 int ring, int q, int r, int T, int TH, int tiles_x, int tiles_y,
                                 unsigned long long* next_item, unsigned* done, unsigned* err,
                                 const __grid_constant__ LifeWindow win) {
+  using G = LifeGeo<R, NW>;
   extern __shared__ __align__(128) uint8_t lsm_raw[];
   uint32_t* win_src = reinterpret_cast<uint32_t*>(lsm_raw);
-  uint32_t* win_dst = reinterpret_cast<uint32_t*>(lsm_raw + kLifeBoxStride);
-  uint32_t* xch = reinterpret_cast<uint32_t*>(lsm_raw + 2 * kLifeBoxStride);
-  uint32_t* Ms = xch + kLifeXchWords;
-  uint32_t* Ds = Ms + kLifeRingWords;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(lsm_raw + static_cast<size_t>(kLifeSmemWords) * 4);
+  uint32_t* win_dst = reinterpret_cast<uint32_t*>(lsm_raw + G::kBoxStride);
+  uint32_t* xch = reinterpret_cast<uint32_t*>(lsm_raw + 2 * G::kBoxStride);
+  uint32_t* Ms = xch + G::kXchWords;
+  uint32_t* Ds = Ms + G::kRingWords;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(lsm_raw + static_cast<size_t>(G::kSmemWords) * 4);
   uint64_t* full = &bars[0];
   uint64_t* empty = &bars[1];
   LifeSlot* slot = reinterpret_cast<LifeSlot*>(&bars[2]);
@@ -295,7 +324,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
   }
   if (tid == 0) {
     mbar_init(full, 1);
-    mbar_init(empty, kLifeWarps);
+    mbar_init(empty, NW);
     fence_barrier_init();
     prefetch_tensormap(&mapX);
     prefetch_tensormap(&mapY);
@@ -307,7 +336,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
   // win.start[j] items; completion counts persist between the launches of a run
   const long long nitems = win.windowed ? win.start[win.np] : static_cast<long long>(win.np) * ntiles;
 
-  if (w == kLifeWarps) {
+  if (w == NW) {
     // ---------------------------------------------------------- producer
     if (lane != 0) return;
     const int dy = (T + TH - 1) / TH;
@@ -330,7 +359,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
       }
       const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
       if (valid && pass > 0) {
-        const unsigned need = static_cast<unsigned>(pass) * kLifeWarps;
+        const unsigned need = static_cast<unsigned>(pass) * NW;
         for (int yy = max(0, ty - dy); yy <= min(tiles_y - 1, ty + dy) && valid; ++yy) {
           for (int xx = max(0, tx - 1); xx <= min(tiles_x - 1, tx + 1) && valid; ++xx) {
             const unsigned* d = &done[yy * tiles_x + xx];
@@ -364,28 +393,28 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
       }
       const int wy0 = ty * TH - T;
       const int gx = tx * kLifeCoreWords - 1;
-      const bool ring_tile = wy0 < ring || wy0 + kLifeWindowRows > H - ring || gx * 32 < ring ||
+      const bool ring_tile = wy0 < ring || wy0 + G::kWindowRows > H - ring || gx * 32 < ring ||
                              (gx + 32) * 32 > W - ring;
       const CUtensorMap* msrc = (pass & 1) ? &mapY : &mapX;
       const CUtensorMap* mdst = (pass & 1) ? &mapX : &mapY;
       // the tiles awaited above wrote through the generic proxy; TMA reads
       // through the async proxy
       fence_proxy_async_global();
-      mbar_arrive_expect_tx(full, kLifeBoxBytes * (ring_tile ? 2u : 1u));
+      mbar_arrive_expect_tx(full, G::kBoxBytes * (ring_tile ? 2u : 1u));
       tma_load_2d(win_src, msrc, gx & ~3, wy0, full);
       if (ring_tile) tma_load_2d(win_dst, mdst, gx & ~3, wy0, full);
     }
   }
 
   // ------------------------------------------------------------ consumers
-  uint32_t* Mw = Ms + w * kLifeRows * 32;
-  uint32_t* Dw = Ds + w * kLifeRows * 32;
+  uint32_t* Mw = Ms + w * R * 32;
+  uint32_t* Dw = Ds + w * R * 32;
   uint32_t full_phase = 0;
   for (;;) {
     // one thread waits (bounded) and the decision is shared, so every
     // consumer warp takes the same path through the named barriers below
     if (tid == 0) s_ok = mbar_wait_bounded(full, full_phase, err) ? 1 : 0;
-    consumers_barrier();
+    consumers_barrier<NW>();
     if (!s_ok) break;
     mbar_try_wait(full, full_phase);  // completed: the TMA data is visible to this thread too
     full_phase ^= 1u;
@@ -399,21 +428,21 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
     const int gx = tx * kLifeCoreWords - 1;
     const int gw = gx + lane;
     const int col = (gx - (gx & ~3)) + lane;  // this lane's word in the box
-    const int gyw = wy0 + w * kLifeRows;      // this warp's row 0
-    const bool ring_tile = wy0 < ring || wy0 + kLifeWindowRows > H - ring || gx * 32 < ring ||
+    const int gyw = wy0 + w * R;      // this warp's row 0
+    const bool ring_tile = wy0 < ring || wy0 + G::kWindowRows > H - ring || gx * 32 < ring ||
                            (gx + 32) * 32 > W - ring;
-    uint32_t x[kLifeRows + 2];
+    uint32_t x[R + 2];
 #pragma unroll
-    for (int i = 0; i < kLifeRows + 2; ++i) x[i] = win_src[(w * kLifeRows + i) * kLifeBoxWords + col];
+    for (int i = 0; i < R + 2; ++i) x[i] = win_src[(w * R + i) * kLifeBoxWords + col];
     if (ring_tile) {
       // interior mask and ring flip of the rows this warp steps (only it reads them)
       const bool gw_in = gw >= 0 && gw < PW;
       const uint32_t colmask = gw_in ? bit_range(ring - 32 * gw, (W - ring) - 32 * gw) : 0u;
 #pragma unroll
-      for (int i = 1; i <= kLifeRows; ++i) {
+      for (int i = 1; i <= R; ++i) {
         const int gy = gyw + i;
         const uint32_t m = (gw_in && gy >= ring && gy < H - ring) ? colmask : 0u;
-        const uint32_t b = win_dst[(w * kLifeRows + i) * kLifeBoxWords + col];
+        const uint32_t b = win_dst[(w * R + i) * kLifeBoxWords + col];
         Mw[(i - 1) * 32 + lane] = m;
         Dw[(i - 1) * 32 + lane] = (x[i] ^ b) & ~m;
       }
@@ -423,20 +452,21 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
     int par = 0;
     for (int s = 0; s < steps; ++s) {
       if (ring_tile) {
-        life_reg_step<true>(x, Mw, Dw, lane);
+        life_reg_step<true, R>(x, Mw, Dw, lane);
       } else {
-        life_reg_step<false>(x, Mw, Dw, lane);
+        life_reg_step<false, R>(x, Mw, Dw, lane);
       }
       if (s + 1 < steps) {
         // exchange the first and last rows with the warps above and below;
-        // two parities, so one barrier per step suffices (a slot is rewritten
-        // two steps later, after every warp has passed the barrier between)
-        uint32_t* xb = xch + par * (2 * kLifeWarps * 32);
+        // two parities, so one meeting per step suffices: a warp rewrites its
+        // slot of a parity two steps later, after meeting its neighbours
+        // again, which they do only once they have read the slot
+        uint32_t* xb = xch + par * (2 * NW * 32);
         xb[(2 * w) * 32 + lane] = x[1];
-        xb[(2 * w + 1) * 32 + lane] = x[kLifeRows];
-        consumers_barrier();
+        xb[(2 * w + 1) * 32 + lane] = x[R];
+        neighbours_barrier<NW>(w);
         if (w > 0) x[0] = xb[(2 * (w - 1) + 1) * 32 + lane];
-        if (w < kLifeWarps - 1) x[kLifeRows + 1] = xb[(2 * (w + 1)) * 32 + lane];
+        if (w < NW - 1) x[R + 1] = xb[(2 * (w + 1)) * 32 + lane];
         par ^= 1;
       }
     }
@@ -445,7 +475,7 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
     const int gc1 = min(H, gc0 + TH);
     if (lane >= 1 && lane <= kLifeCoreWords && gw < PW) {
 #pragma unroll
-      for (int i = 1; i <= kLifeRows; ++i) {
+      for (int i = 1; i <= R; ++i) {
         const int gy = gyw + i;
         if (gy >= gc0 && gy < gc1) dst[static_cast<int64_t>(gy) * PW + gw] = x[i];
       }
@@ -458,15 +488,49 @@ __global__ void __launch_bounds__(kLifeThreads, 2)
 
 }  // namespace
 
+namespace {
+
+// Kernel variants: rows per lane, consumer warps, blocks per SM.
+struct LifeVariant {
+  int R, NW, min_blocks;
+  int threads, window_rows;
+  size_t smem;
+};
+template <int R, int NW, int MB>
+constexpr LifeVariant variant_of() {
+  return LifeVariant{R, NW, MB, LifeGeo<R, NW>::kThreads, LifeGeo<R, NW>::kWindowRows, LifeGeo<R, NW>::kSmemBytes};
+}
+constexpr LifeVariant kLifeVariants[] = {variant_of<8, 15, 2>(), variant_of<16, 15, 1>(), variant_of<16, 7, 2>()};
+
+int life_variant_index() {
+  static const int k = [] {
+    const char* e = std::getenv("PSKEL_LIFE_VARIANT");
+    const int v = e ? std::atoi(e) : 0;
+    return (v >= 0 && v < 3) ? v : 0;
+  }();
+  return k;
+}
+const LifeVariant& life_variant() { return kLifeVariants[life_variant_index()]; }
+
+const void* life_kernel_ptr(int k) {
+  switch (k) {
+    case 1: return reinterpret_cast<const void*>(life_bits_persistent_kernel<16, 15, 1>);
+    case 2: return reinterpret_cast<const void*>(life_bits_persistent_kernel<16, 7, 2>);
+    default: return reinterpret_cast<const void*>(life_bits_persistent_kernel<8, 15, 2>);
+  }
+}
+
+}  // namespace
+
 int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
 
 int life_bits_tiles_x(int W) { return (life_bits_words(W) + kLifeCoreWords - 1) / kLifeCoreWords; }
 
-int life_bits_max_tile_h(int T) { return kLifeWindowRows - 2 * T; }
+int life_bits_max_tile_h(int T) { return life_variant().window_rows - 2 * T; }
 
 int life_bits_tiles(int W, int H, int TH) { return life_bits_tiles_x(W) * ((H + TH - 1) / TH); }
 
-size_t life_bits_smem_bytes() { return kLifeSmemBytes; }
+size_t life_bits_smem_bytes() { return life_variant().smem; }
 
 
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
@@ -504,12 +568,10 @@ size_t life_bits_sync_bytes(int W, int H, int TH) {
 
 int life_bits_persistent_ctas_per_sm() {
   int n = 0;
-  const size_t smem = life_bits_smem_bytes();
-  cudaFuncSetAttribute(life_bits_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       static_cast<int>(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_bits_persistent_kernel, kLifeThreads, smem) !=
-      cudaSuccess)
-    return 1;
+  const LifeVariant& v = life_variant();
+  const void* k = life_kernel_ptr(life_variant_index());
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(v.smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, v.threads, v.smem) != cudaSuccess) return 1;
   return n > 0 ? n : 1;
 }
 
@@ -547,12 +609,24 @@ cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int rin
   CUtensorMap mx, my;
   const uint64_t dims[2] = {static_cast<uint64_t>(PW), static_cast<uint64_t>(H)};
   const uint64_t strides[1] = {static_cast<uint64_t>(PW) * 4};
-  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(kLifeWindowRows)};
+  const LifeVariant& v = life_variant();
+  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(v.window_rows)};
   cudaError_t e = encode_tmap(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, X, dims, strides, box);
   if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
   if (e != cudaSuccess) return e;
-  life_bits_persistent_kernel<<<ctas, kLifeThreads, life_bits_smem_bytes(), s>>>(
-      mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y, next, done, err, win);
+  switch (life_variant_index()) {
+    case 1:
+      life_bits_persistent_kernel<16, 15, 1><<<ctas, v.threads, v.smem, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH,
+                                                                            tiles_x, tiles_y, next, done, err, win);
+      break;
+    case 2:
+      life_bits_persistent_kernel<16, 7, 2><<<ctas, v.threads, v.smem, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH,
+                                                                           tiles_x, tiles_y, next, done, err, win);
+      break;
+    default:
+      life_bits_persistent_kernel<8, 15, 2><<<ctas, v.threads, v.smem, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH,
+                                                                           tiles_x, tiles_y, next, done, err, win);
+  }
   return cudaGetLastError();
 }
 

@@ -772,6 +772,12 @@ cudaError_t stream3d_tma_step(int dtype, const CUtensorMap* map, const Stencil3D
   return cudaGetLastError();
 }
 
+cudaError_t stream3d_reduce_residuals(const double* partials, int ctas, int steps, int64_t step0, int every,
+                                      double* residuals, cudaStream_t s) {
+  reduce3d_residual<<<steps, 256, 0, s>>>(partials, ctas, steps, step0, every, residuals);
+  return cudaGetLastError();
+}
+
 cudaError_t stream3d_step(int dtype, const Stencil3DParams& p, cudaStream_t s) {
   if (dtype == 2) return p.nm == 7 ? launch_stream<__nv_bfloat16, 7>(p, s) : launch_stream<__nv_bfloat16, 0>(p, s);
   return p.nm == 7 ? launch_stream<float, 7>(p, s) : launch_stream<float, 0>(p, s);

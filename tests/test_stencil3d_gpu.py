@@ -80,6 +80,26 @@ def test_heat3d_streaming_items(cuda, oracle_mod, dtype, W, H, D, th, ctas, halo
     np.testing.assert_allclose(res, wres, rtol=RES_RTOL, atol=0)
 
 
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("W,H,D", [(40, 33, 72), (17, 50, 264), (300, 7, 8), (16, 3, 256)])
+@pytest.mark.parametrize("th,ctas", [(0, 0), (3, 1), (64, 5), (1, 0)])
+@pytest.mark.parametrize("halo", [0.0, -0.0, 0.5])
+@pytest.mark.parametrize("iters,every", [(6, 3), (7, 1), (9, 0)])
+def test_heat3d_two_step_streaming(cuda, oracle_mod, dtype, W, H, D, th, ctas, halo, iters, every):
+    # two steps per launch (stream3d_tb.cu): the second step fused behind the
+    # first in shared memory; ragged w and d blocks, work items of th planes,
+    # few persistent blocks; residuals reported by either step of a pass (and
+    # by both, every=1); even and odd iteration counts (an even number of
+    # two-step passes, the rest one-step passes)
+    keep = P._Keep()
+    a, b = grids(W, H, D, W * H + D + iters, dtype)
+    sch = dict(time_steps=2, tile_w=0, tile_h=th, tile_d=0, ctas=ctas)
+    got, res = run3d(cuda, heat(keep, dtype, halo=halo), a, b, iters, sched=sch, every=every, dtype=dtype)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, S.HEAT7_WEIGHTS, iters, halo=halo, dtype=dtype, every=every)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
+
+
 @pytest.mark.parametrize("T,tw,td,th", [(1, 0, 0, 0), (2, 16, 32, 0), (3, 8, 16, 5), (4, 32, 64, 7), (8, 8, 8, 0),
                                         (2, 0, 0, 1), (3, 16, 16, 13)])
 def test_heat3d_schedules(cuda, oracle_mod, T, tw, td, th):

@@ -112,7 +112,7 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
 // is split exactly into hi + lo (Knuth's TwoSum), hi^2 exactly into p + e
 // (FMA), and p is added to the running (s, c) pair with TwoSum; the 2*hi*lo
 // term and the pair's low part are added in fp32. Relative error of the sum is
-// about 2^-44 -- fp64 accumulation of exact differences gives 2^-53 per add.
+// about 2^-44 per term; flush() hands the pair to an fp64 sum every plane.
 struct SqDiffAcc {
   float s = 0.0f, c = 0.0f;
   __device__ __forceinline__ void add(float a, float b) {
@@ -129,6 +129,14 @@ struct SqDiffAcc {
     c = __fadd_rn(c, __fadd_rn(err, __fadd_rn(e, __fmul_rn(__fmul_rn(2.0f, hi), lo))));
   }
   __device__ __forceinline__ double value() const { return static_cast<double>(s) + static_cast<double>(c); }
+  // Moves the pair into an fp64 sum and restarts it. Called once per plane,
+  // so that a pair sums a few dozen terms and the fp64 pipe adds once per
+  // thread and plane.
+  __device__ __forceinline__ void flush(double& total) {
+    total += value();
+    s = 0.0f;
+    c = 0.0f;
+  }
 };
 
 // Storage conversions. fp32 storage is the identity; bf16 storage widens on

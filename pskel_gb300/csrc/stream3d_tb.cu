@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
   const int64_t plane = static_cast<int64_t>(W) * D;
   const bool edge = warp == kTbEdge;
   SqDiffAcc acc1, acc2;
+  double tot1 = 0.0, tot2 = 0.0;
   uint32_t n0 = 0, n1 = 0;  // source planes consumed / level-1 planes computed by this block
   auto l0p = [&](uint32_t n) -> const uint8_t* { return l0 + (n % kTbL0Slots) * kTbL0Bytes; };
   auto l1p = [&](uint32_t n) -> uint8_t* { return l1 + (n % kTbL1Slots) * kTbL1Bytes; };
@@ -271,6 +272,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           }
           sts(L1w + (rb + 1 + j) * kTbRowBytes + vo, o);
         }
+        if (kRep & 1) acc1.flush(tot1);
       } else if (ok) {
         // the edge warp: rows w0-1 and w0+16 of level 1 ...
 #pragma unroll
@@ -386,6 +388,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
             }
           }
         }
+        if (kRep & 2) acc2.flush(tot2);
       }
       ++n1;
     }
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
     n0 += static_cast<uint32_t>(h1 - h0 + 4);
   }
   if constexpr (kRep != 0) {
-    double v1 = acc1.value(), v2 = acc2.value();
+    double v1 = tot1, v2 = tot2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       v1 += __shfl_down_sync(0xFFFFFFFFu, v1, o);

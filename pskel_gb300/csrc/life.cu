@@ -31,8 +31,6 @@
 // refreshed) and at lanes 0 and 31 (no neighbour lane) and advances one cell
 // per step, so after T <= 31 steps rows T .. T + TH - 1 of the window and
 // lanes 1..30 are exact.
-#include <cstdlib>
-
 #include "common.cuh"
 #include "kernels.h"
 
@@ -490,35 +488,15 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
 
 namespace {
 
-// Kernel variants: rows per lane, consumer warps, blocks per SM.
-struct LifeVariant {
-  int R, NW, min_blocks;
-  int threads, window_rows;
-  size_t smem;
-};
-template <int R, int NW, int MB>
-constexpr LifeVariant variant_of() {
-  return LifeVariant{R, NW, MB, LifeGeo<R, NW>::kThreads, LifeGeo<R, NW>::kWindowRows, LifeGeo<R, NW>::kSmemBytes};
-}
-constexpr LifeVariant kLifeVariants[] = {variant_of<8, 15, 2>(), variant_of<16, 15, 1>(), variant_of<16, 7, 2>()};
-
-int life_variant_index() {
-  static const int k = [] {
-    const char* e = std::getenv("PSKEL_LIFE_VARIANT");
-    const int v = e ? std::atoi(e) : 0;
-    return (v >= 0 && v < 3) ? v : 0;
-  }();
-  return k;
-}
-const LifeVariant& life_variant() { return kLifeVariants[life_variant_index()]; }
-
-const void* life_kernel_ptr(int k) {
-  switch (k) {
-    case 1: return reinterpret_cast<const void*>(life_bits_persistent_kernel<16, 15, 1>);
-    case 2: return reinterpret_cast<const void*>(life_bits_persistent_kernel<16, 7, 2>);
-    default: return reinterpret_cast<const void*>(life_bits_persistent_kernel<8, 15, 2>);
-  }
-}
+// The kernel as launched: kLifeRows rows per lane, kLifeWarps consumer warps,
+// one block per SM. Measured on GB300 (8192^2, 1000 generations): 16 rows x
+// 15 warps at one block per SM 27.3 T updates/s (T = 15); 8 rows x 15 warps
+// at two blocks per SM 21.5 T (T = 7, the best T for it; its windows are half
+// as tall, so the halo rows and the per-step exchange cost twice as much per
+// row); 16 rows x 7 warps at two blocks per SM 22.5 T.
+using LifeKernelGeo = LifeGeo<kLifeRows, kLifeWarps>;
+constexpr int kLifeMinBlocks = 1;
+const auto life_kernel = life_bits_persistent_kernel<kLifeRows, kLifeWarps, kLifeMinBlocks>;
 
 }  // namespace
 
@@ -526,11 +504,11 @@ int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
 
 int life_bits_tiles_x(int W) { return (life_bits_words(W) + kLifeCoreWords - 1) / kLifeCoreWords; }
 
-int life_bits_max_tile_h(int T) { return life_variant().window_rows - 2 * T; }
+int life_bits_max_tile_h(int T) { return LifeKernelGeo::kWindowRows - 2 * T; }
 
 int life_bits_tiles(int W, int H, int TH) { return life_bits_tiles_x(W) * ((H + TH - 1) / TH); }
 
-size_t life_bits_smem_bytes() { return life_variant().smem; }
+size_t life_bits_smem_bytes() { return LifeKernelGeo::kSmemBytes; }
 
 
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
@@ -568,10 +546,10 @@ size_t life_bits_sync_bytes(int W, int H, int TH) {
 
 int life_bits_persistent_ctas_per_sm() {
   int n = 0;
-  const LifeVariant& v = life_variant();
-  const void* k = life_kernel_ptr(life_variant_index());
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(v.smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, v.threads, v.smem) != cudaSuccess) return 1;
+  const size_t smem = LifeKernelGeo::kSmemBytes;
+  cudaFuncSetAttribute(life_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_kernel, LifeKernelGeo::kThreads, smem) != cudaSuccess)
+    return 1;
   return n > 0 ? n : 1;
 }
 
@@ -609,24 +587,12 @@ cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int rin
   CUtensorMap mx, my;
   const uint64_t dims[2] = {static_cast<uint64_t>(PW), static_cast<uint64_t>(H)};
   const uint64_t strides[1] = {static_cast<uint64_t>(PW) * 4};
-  const LifeVariant& v = life_variant();
-  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(v.window_rows)};
+  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(LifeKernelGeo::kWindowRows)};
   cudaError_t e = encode_tmap(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, X, dims, strides, box);
   if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
   if (e != cudaSuccess) return e;
-  switch (life_variant_index()) {
-    case 1:
-      life_bits_persistent_kernel<16, 15, 1><<<ctas, v.threads, v.smem, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH,
-                                                                            tiles_x, tiles_y, next, done, err, win);
-      break;
-    case 2:
-      life_bits_persistent_kernel<16, 7, 2><<<ctas, v.threads, v.smem, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH,
-                                                                           tiles_x, tiles_y, next, done, err, win);
-      break;
-    default:
-      life_bits_persistent_kernel<8, 15, 2><<<ctas, v.threads, v.smem, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH,
-                                                                           tiles_x, tiles_y, next, done, err, win);
-  }
+  life_kernel<<<ctas, LifeKernelGeo::kThreads, LifeKernelGeo::kSmemBytes, s>>>(
+      mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y, next, done, err, win);
   return cudaGetLastError();
 }
 

@@ -435,14 +435,17 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
     return;
   }
 
-  // ---- consumers: each staged plane is read from shared memory (and, for
-  // bf16, widened) once, when it arrives as the upper plane; its values then
-  // roll through registers as the centre plane and the lower plane of the
-  // next two output planes. The centre plane's outer rows (w-1, w+kRW) and
-  // edge cells are read while it is the centre, after which its slot is free.
+  // ---- consumers
   const int64_t plane = static_cast<int64_t>(W) * D;
   TS* __restrict__ dst = static_cast<TS*>(p.dst);
   const float halo = p.halo;
+  uint32_t hraw;
+  if constexpr (sizeof(TS) == 4) {
+    hraw = __float_as_uint(halo);
+  } else {
+    const uint32_t hb = __bfloat16_as_ushort(__float2bfloat16_rn(halo));
+    hraw = hb | (hb << 16);
+  }
   // this thread's staged rows: row 0 of the box is w0-1
   const int r0 = kRW * warp + 1;
   const uint8_t* const sbase = smem_raw;
@@ -451,17 +454,12 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
   const int o_er = r0 * kS3RowBytes + 33 * 16;                                  // d0+32V
   SqDiffAcc acc_res;
   double acc_total = 0.0;
-  // the V cells of the vector at `off` of `slot`, widened; the halo value
-  // instead when `in` is false
-  auto ldf = [&](int slot, int off, bool in, float (&f)[V]) {
-    Vt v;
+  auto ld = [&](int slot, int off, Vt& v) {
     const uint4 x = *reinterpret_cast<const uint4*>(sbase + slot * kS3PlaneBytes + off);
     v.r[0] = x.x;
     v.r[1] = x.y;
     v.r[2] = x.z;
     v.r[3] = x.w;
-#pragma unroll
-    for (int c = 0; c < V; ++c) f[c] = (kZeroHalo || in) ? v.at(c) : halo;
   };
   auto ld1 = [&](int slot, int off) -> float {
     return S::load(*reinterpret_cast<const TS*>(sbase + slot * kS3PlaneBytes + off));
@@ -485,33 +483,26 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
     // general halo: which staged values lie outside the grid
     const bool wm_in = row_ok[0] && w > 0, wp_in = row_ok[kRW - 1] && w + kRW < W;
     const bool el_in = d0 > 0, er_in = d0 + 32 * V < D;
-    int s_dn = s_next, s_cur = next(s_dn);
-    uint32_t ph_dn = ph_next, ph_cur = ph_next ^ (s_cur == 0 ? 1u : 0u);
+    int s_dn = s_next, s_cur = next(s_dn), s_up = next(s_cur);
+    uint32_t ph_dn = ph_next, ph_cur = ph_next ^ (s_cur == 0 ? 1u : 0u), ph_up = ph_cur ^ (s_up == 0 ? 1u : 0u);
     if (!wait_full(s_dn, ph_dn) || !wait_full(s_cur, ph_cur)) {
       alive = false;
       break;
     }
-    float dnf[kRW][V], curf[kRW][V];
-#pragma unroll
-    for (int j = 0; j < kRW; ++j) {
-      ldf(s_dn, o_row0 + j * kS3RowBytes, row_ok[j] && h0 - 1 >= 0, dnf[j]);
-      ldf(s_cur, o_row0 + j * kS3RowBytes, row_ok[j], curf[j]);
-    }
-    // plane h0-1 has been read
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s_dn]);
-    int s_up = next(s_cur);
-    uint32_t ph_up = ph_cur ^ (s_up == 0 ? 1u : 0u);
     for (int h = h0; h < h1; ++h) {
       if (!wait_full(s_up, ph_up)) {
         alive = false;
         break;
       }
-      float upf[kRW][V], wmf[V], wpf[V];
+      Vt dn[kRW], cur[kRW], up[kRW], wm, wp;
 #pragma unroll
-      for (int j = 0; j < kRW; ++j) ldf(s_up, o_row0 + j * kS3RowBytes, row_ok[j] && h + 1 < H, upf[j]);
-      ldf(s_cur, o_row0 - kS3RowBytes, wm_in, wmf);
-      ldf(s_cur, o_row0 + kRW * kS3RowBytes, wp_in, wpf);
+      for (int j = 0; j < kRW; ++j) {
+        ld(s_dn, o_row0 + j * kS3RowBytes, dn[j]);
+        ld(s_cur, o_row0 + j * kS3RowBytes, cur[j]);
+        ld(s_up, o_row0 + j * kS3RowBytes, up[j]);
+      }
+      ld(s_cur, o_row0 - kS3RowBytes, wm);
+      ld(s_cur, o_row0 + kRW * kS3RowBytes, wp);
       float el[kRW], er[kRW];
 #pragma unroll
       for (int j = 0; j < kRW; ++j) {
@@ -520,24 +511,40 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
       }
       if (lane == 0) {
 #pragma unroll
-        for (int j = 0; j < kRW; ++j) el[j] = (kZeroHalo || el_in) ? ld1(s_cur, o_el + j * kS3RowBytes) : halo;
+        for (int j = 0; j < kRW; ++j) el[j] = ld1(s_cur, o_el + j * kS3RowBytes);
       }
       if (lane == 31) {
 #pragma unroll
-        for (int j = 0; j < kRW; ++j) er[j] = (kZeroHalo || er_in) ? ld1(s_cur, o_er + j * kS3RowBytes) : halo;
+        for (int j = 0; j < kRW; ++j) er[j] = ld1(s_cur, o_er + j * kS3RowBytes);
       }
-      // plane h (the centre) has been read for the last time
+      // plane h-1 is read for the last time
       __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[s_cur]);
+      if (lane == 0) mbar_arrive(&empty[s_dn]);
+      if constexpr (!kZeroHalo) {
+#pragma unroll
+        for (int j = 0; j < kRW; ++j) {
+          if (h - 1 < 0) dn[j].fill(hraw);
+          if (h + 1 >= H) up[j].fill(hraw);
+          if (!row_ok[j]) {
+            dn[j].fill(hraw);
+            cur[j].fill(hraw);
+            up[j].fill(hraw);
+          }
+          if (!el_in) el[j] = halo;
+          if (!er_in) er[j] = halo;
+        }
+        if (!wm_in) wm.fill(hraw);
+        if (!wp_in) wp.fill(hraw);
+      }
       TS* out = dst + (h * plane + static_cast<int64_t>(w) * D + d);
 #pragma unroll
       for (int j = 0; j < kRW; ++j) {
-        float dl = __shfl_up_sync(0xFFFFFFFFu, curf[j][V - 1], 1);
-        float dr = __shfl_down_sync(0xFFFFFFFFu, curf[j][0], 1);
+        float dl = __shfl_up_sync(0xFFFFFFFFu, cur[j].at(V - 1), 1);
+        float dr = __shfl_down_sync(0xFFFFFFFFu, cur[j].at(0), 1);
         if (lane == 0) dl = el[j];
         if (lane == 31) dr = er[j];
-        const float(&a)[V] = (j == 0) ? wmf : curf[j > 0 ? j - 1 : 0];
-        const float(&b)[V] = (j == kRW - 1) ? wpf : curf[j < kRW - 1 ? j + 1 : 0];
+        const Vt& a = (j == 0) ? wm : cur[j > 0 ? j - 1 : 0];
+        const Vt& b = (j == kRW - 1) ? wp : cur[j < kRW - 1 ? j + 1 : 0];
         uint32_t o[4];
 #pragma unroll
         for (int g = 0; g < V / 4; ++g) {
@@ -545,13 +552,13 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const int c = 4 * g + k;
-            const float l = (c == 0) ? dl : curf[j][c - 1];
-            const float r = (c == V - 1) ? dr : curf[j][c + 1];
-            float acc = __fmul_rn(p.wt[0], curf[j][c]);
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[1], dnf[j][c]));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[2], upf[j][c]));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[3], a[c]));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[4], b[c]));
+            const float l = (c == 0) ? dl : cur[j].at(c - 1);
+            const float r = (c == V - 1) ? dr : cur[j].at(c + 1);
+            float acc = __fmul_rn(p.wt[0], cur[j].at(c));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[1], dn[j].at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[2], up[j].at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[3], a.at(c)));
+            acc = __fadd_rn(acc, __fmul_rn(p.wt[4], b.at(c)));
             acc = __fadd_rn(acc, __fmul_rn(p.wt[5], l));
             acc = __fadd_rn(acc, __fmul_rn(p.wt[6], r));
             res[k] = acc;
@@ -574,30 +581,26 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
           }
           if (kReport && row_ok[j]) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) acc_res.add(stored[k], curf[j][4 * g + k]);
+            for (int k = 0; k < 4; ++k) acc_res.add(stored[k], cur[j].at(4 * g + k));
           }
         }
         if (row_ok[j]) *reinterpret_cast<uint4*>(out + j * D) = make_uint4(o[0], o[1], o[2], o[3]);
       }
       if (kReport) acc_res.flush(acc_total);
-      // roll: the centre becomes the lower plane, the upper plane the centre
-#pragma unroll
-      for (int j = 0; j < kRW; ++j) {
-#pragma unroll
-        for (int c = 0; c < V; ++c) {
-          dnf[j][c] = curf[j][c];
-          curf[j][c] = upf[j][c];
-        }
-      }
+      s_dn = s_cur;
+      ph_dn = ph_cur;
       s_cur = s_up;
       ph_cur = ph_up;
       s_up = next(s_up);
       ph_up ^= (s_up == 0) ? 1u : 0u;
     }
     if (!alive) break;
-    // plane h1 (read as the last upper plane) is released at the end of the item
+    // planes h1-1 and h1 are released at the end of the item
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s_cur]);
+    if (lane == 0) {
+      mbar_arrive(&empty[s_dn]);
+      mbar_arrive(&empty[s_cur]);
+    }
     s_next = s_up;
     ph_next = ph_up;
   }

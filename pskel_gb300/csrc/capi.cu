@@ -222,7 +222,7 @@ static bool tma_ok(const void* p, int64_t pitch_bytes) {
 // planes, and the final plane's interior is unpacked into the result buffer.
 // The other buffer is not written; ring cells of the result keep their bytes.
 // Generations per pass of the Life kernel by default (measured on GB300, 8192^2).
-constexpr int kLifeDefaultSteps = 15;
+constexpr int kLifeDefaultSteps = 13;
 
 static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
                                  int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,
@@ -629,9 +629,11 @@ static bool cross7_ok(const pskel_stencil& st, const void* in, const void* out, 
          (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0;
 }
 
-// Steps per pass of the 7-point cross by default: two (one HBM round trip per
-// two steps; measured on GB300).
-constexpr int kCross7DefaultSteps = 2;
+// Steps per pass of the 7-point cross by default, measured on GB300 (512^3,
+// 50 steps): fp32 two (one HBM round trip per two steps: 844 against 787
+// GCells/s at one step per launch); bf16 one (the one-step kernel is bound by
+// HBM at half the bytes and runs 1179 against 1048 for two steps).
+static int cross7_default_steps(pskel_dtype dt) { return dt == PSKEL_F32 ? 2 : 1; }
 
 // Per-pass lengths of a two-step run: an even number of two-step passes and
 // the rest one-step passes, so that the pass count has the parity of `iters`
@@ -787,7 +789,7 @@ pskel_status iterate3d(const pskel_stencil& st, void* in, void* out, int64_t W, 
   const size_t esz = dtype_size(st.dtype);
   const int vec = static_cast<int>(16 / esz);
   const bool cross7 = cross7_ok(st, in, out, D);
-  int T = (sched && sched->time_steps > 0) ? sched->time_steps : (cross7 ? kCross7DefaultSteps : 1);
+  int T = (sched && sched->time_steps > 0) ? sched->time_steps : (cross7 ? cross7_default_steps(st.dtype) : 1);
   T = static_cast<int>(std::min<int64_t>(std::min(T, kMax3DSteps), std::max<int64_t>(iters, 1)));
   if (R == 0) T = 1;
   if (T == 1 || (T == 2 && cross7))

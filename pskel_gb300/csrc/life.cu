@@ -493,7 +493,9 @@ namespace {
 // 15 warps at one block per SM 27.3 T updates/s (T = 15); 8 rows x 15 warps
 // at two blocks per SM 21.5 T (T = 7, the best T for it; its windows are half
 // as tall, so the halo rows and the per-step exchange cost twice as much per
-// row); 16 rows x 7 warps at two blocks per SM 22.5 T.
+// row); 16 rows x 7 warps at two blocks per SM 22.5 T. The row shifts as
+// integer multiply-adds on the idle FMA pipe (by 2 and 2^31 from a kernel
+// argument) instead of funnel shifts on the ALU pipe: 23.3 T.
 using LifeKernelGeo = LifeGeo<kLifeRows, kLifeWarps>;
 constexpr int kLifeMinBlocks = 1;
 const auto life_kernel = life_bits_persistent_kernel<kLifeRows, kLifeWarps, kLifeMinBlocks>;

@@ -5,10 +5,10 @@
 // cells) x 16 w rows x HC planes, as the one-step kernel does. A producer
 // warp streams the source planes h0-2 .. h1+1 of its items by 3D TMA (boxes
 // of 34 vectors x 20 rows: two rows and a vector of halo on each side, zero
-// outside the grid) into a ring of 3 slots. For each plane p = h0-1 .. h1
+// outside the grid) into a ring of 4 slots. For each plane p = h0-1 .. h1
 // the block computes the first step (level 1) of plane p over 18 rows
 // (w0-1 .. w0+16) and the two edge cells d0-1 and d0+32V of the 16 core rows
-// into a ring of 4 level-1 planes in shared memory, and then the second step
+// into a ring of 3 level-1 planes in shared memory, and then the second step
 // (level 2) of plane p-1 over the core from level-1 planes p-2, p-1, p, which
 // goes to HBM. HBM therefore sees one read and one write of the grid per two
 // steps. Level-1 values are rounded to the storage type, as the step-by-step
@@ -17,9 +17,9 @@
 //
 // Warps: 4 consumer warps (level 1 and level 2 of 4 core rows each), an edge
 // warp (level 1 of the rows w0-1 and w0+16 and of the 32 edge cells), the
-// producer. One named barrier per plane between level 1 and level 2; the
-// level-1 ring has 4 slots so that a warp may write plane p+1 while another
-// still reads p-2 .. p. Every wait is bounded.
+// producer. Two named barriers per plane: between level 1 and level 2, and
+// after level 2, before level 1 of the next plane overwrites the oldest of the
+// three level-1 slots. Every wait is bounded.
 //
 // Arithmetic: the reference's order (centre, h-1, h+1, w-1, w+1, d-1, d+1),
 // __fmul_rn / __fadd_rn, no contraction: bit-identical to two launches of the
@@ -39,8 +39,8 @@ constexpr int kTbL0Rows = 20;                // w0-2 .. w0+17
 constexpr int kTbL1Rows = 18;                // w0-1 .. w0+16
 constexpr int kTbL0Bytes = (kTbRowBytes * kTbL0Rows + 127) & ~127;
 constexpr int kTbL1Bytes = (kTbRowBytes * kTbL1Rows + 127) & ~127;
-constexpr int kTbL0Slots = 3;
-constexpr int kTbL1Slots = 4;
+constexpr int kTbL0Slots = 4;
+constexpr int kTbL1Slots = 3;
 constexpr int kTbCons = 4;                   // consumer warps, 4 core rows each
 constexpr int kTbRW = 4;
 constexpr int kTbEdge = kTbCons;             // warp index of the edge warp
@@ -219,51 +219,46 @@ __global__ void __launch_bounds__(kTbThreads, 3)
       const bool dn_in = pl - 1 >= 0, up_in = pl + 1 < H;
       // ---------------- level 1 of plane pl
       if (ok && !edge) {
-        // rows r = 4 warp + j (0..15): staged rows r+1 .. r+6 of the centre plane
+        // rows r = 4 warp + j (0..15), one at a time with a rolling window of
+        // three centre-plane rows (staged rows r+1 .. r+3): few vectors live
         const int rb = kTbRW * warp;
-        Vt dn[kTbRW], up[kTbRW], cur[kTbRW + 2];
-        float el[kTbRW], er[kTbRW];
-#pragma unroll
-        for (int j = 0; j < kTbRW; ++j) {
-          lds(Ldn + (rb + 2 + j) * kTbRowBytes + vo, dn[j]);
-          lds(Lup + (rb + 2 + j) * kTbRowBytes + vo, up[j]);
-          el[j] = ld_cell<TS>(Lcur + (rb + 2 + j) * kTbRowBytes + (V - 1) * ES);
-          er[j] = ld_cell<TS>(Lcur + (rb + 2 + j) * kTbRowBytes + 33 * 16);
-        }
-#pragma unroll
-        for (int j = 0; j < kTbRW + 2; ++j) lds(Lcur + (rb + 1 + j) * kTbRowBytes + vo, cur[j]);
+        Vt a, c;
+        lds(Lcur + (rb + 1) * kTbRowBytes + vo, a);
+        lds(Lcur + (rb + 2) * kTbRowBytes + vo, c);
         if constexpr (!kZeroHalo) {
-#pragma unroll
-          for (int j = 0; j < kTbRW + 2; ++j) {
-            const int w = w0 + rb - 1 + j;
-            if (!d_ok || w < 0 || w >= W) cur[j].fill(hraw);
-          }
-#pragma unroll
-          for (int j = 0; j < kTbRW; ++j) {
-            const int w = w0 + rb + j;
-            if (!dn_in || !d_ok || w >= W) dn[j].fill(hraw);
-            if (!up_in || !d_ok || w >= W) up[j].fill(hraw);
-            if (!el_in) el[j] = halo;
-            if (!er_in) er[j] = halo;
-          }
+          if (!d_ok || w0 + rb - 1 < 0 || w0 + rb - 1 >= W) a.fill(hraw);
+          if (!d_ok || w0 + rb >= W) c.fill(hraw);
         }
 #pragma unroll
         for (int j = 0; j < kTbRW; ++j) {
-          const Vt& c = cur[j + 1];
+          const int w = w0 + rb + j;
+          Vt b, dn, up;
+          lds(Lcur + (rb + 3 + j) * kTbRowBytes + vo, b);
+          lds(Ldn + (rb + 2 + j) * kTbRowBytes + vo, dn);
+          lds(Lup + (rb + 2 + j) * kTbRowBytes + vo, up);
+          float el = ld_cell<TS>(Lcur + (rb + 2 + j) * kTbRowBytes + (V - 1) * ES);
+          float er = ld_cell<TS>(Lcur + (rb + 2 + j) * kTbRowBytes + 33 * 16);
+          if constexpr (!kZeroHalo) {
+            if (!d_ok || w + 1 >= W) b.fill(hraw);
+            if (!dn_in || !d_ok || w >= W) dn.fill(hraw);
+            if (!up_in || !d_ok || w >= W) up.fill(hraw);
+            if (!el_in) el = halo;
+            if (!er_in) er = halo;
+          }
           float dl = __shfl_up_sync(0xFFFFFFFFu, c.at(V - 1), 1);
           float dr = __shfl_down_sync(0xFFFFFFFFu, c.at(0), 1);
-          if (lane == 0) dl = el[j];
-          if (lane == 31) dr = er[j];
+          if (lane == 0) dl = el;
+          if (lane == 31) dr = er;
           float res[V], stored[V];
 #pragma unroll
           for (int k = 0; k < V; ++k) {
             const float l = (k == 0) ? dl : c.at(k - 1);
             const float r = (k == V - 1) ? dr : c.at(k + 1);
-            res[k] = cross7(wt, c.at(k), dn[j].at(k), up[j].at(k), cur[j].at(k), cur[j + 2].at(k), l, r);
+            res[k] = cross7(wt, c.at(k), dn.at(k), up.at(k), a.at(k), b.at(k), l, r);
           }
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
-          const bool valid = plane_in && d_ok && w0 + rb + j < W;
+          const bool valid = plane_in && d_ok && w < W;
           if (!valid) {
             o[0] = o[1] = o[2] = o[3] = hraw;
           } else if ((kRep & 1) && pl >= h0 && pl < h1) {
@@ -271,6 +266,8 @@ __global__ void __launch_bounds__(kTbThreads, 3)
             for (int k = 0; k < V; ++k) acc1.add(stored[k], c.at(k));
           }
           sts(L1w + (rb + 1 + j) * kTbRowBytes + vo, o);
+          a = c;
+          c = b;
         }
         if (kRep & 1) acc1.flush(tot1);
       } else if (ok) {
@@ -352,31 +349,30 @@ __global__ void __launch_bounds__(kTbThreads, 3)
         const uint8_t* Mcur = l1p(n1 - 1);
         const uint8_t* Mup = l1p(n1);
         const int rb = kTbRW * warp;
-        Vt dn[kTbRW], up[kTbRW], cur[kTbRW + 2];
-        float el[kTbRW], er[kTbRW];
-#pragma unroll
-        for (int j = 0; j < kTbRW; ++j) {
-          lds(Mdn + (rb + 1 + j) * kTbRowBytes + vo, dn[j]);
-          lds(Mup + (rb + 1 + j) * kTbRowBytes + vo, up[j]);
-          el[j] = ld_cell<TS>(Mcur + (rb + 1 + j) * kTbRowBytes + (V - 1) * ES);
-          er[j] = ld_cell<TS>(Mcur + (rb + 1 + j) * kTbRowBytes + 33 * 16);
-        }
-#pragma unroll
-        for (int j = 0; j < kTbRW + 2; ++j) lds(Mcur + (rb + j) * kTbRowBytes + vo, cur[j]);
+        // level-1 rows are stored at row index r+1; cells outside the grid hold
+        // the halo value already
+        Vt a, c;
+        lds(Mcur + rb * kTbRowBytes + vo, a);
+        lds(Mcur + (rb + 1) * kTbRowBytes + vo, c);
         TS* out = dst + (static_cast<int64_t>(pl - 1) * plane + static_cast<int64_t>(w0 + rb) * D + d);
 #pragma unroll
         for (int j = 0; j < kTbRW; ++j) {
-          const Vt& c = cur[j + 1];
+          Vt b, dn, up;
+          lds(Mcur + (rb + 2 + j) * kTbRowBytes + vo, b);
+          lds(Mdn + (rb + 1 + j) * kTbRowBytes + vo, dn);
+          lds(Mup + (rb + 1 + j) * kTbRowBytes + vo, up);
+          const float el = ld_cell<TS>(Mcur + (rb + 1 + j) * kTbRowBytes + (V - 1) * ES);
+          const float er = ld_cell<TS>(Mcur + (rb + 1 + j) * kTbRowBytes + 33 * 16);
           float dl = __shfl_up_sync(0xFFFFFFFFu, c.at(V - 1), 1);
           float dr = __shfl_down_sync(0xFFFFFFFFu, c.at(0), 1);
-          if (lane == 0) dl = el[j];
-          if (lane == 31) dr = er[j];
+          if (lane == 0) dl = el;
+          if (lane == 31) dr = er;
           float res[V], stored[V];
 #pragma unroll
           for (int k = 0; k < V; ++k) {
             const float l = (k == 0) ? dl : c.at(k - 1);
             const float r = (k == V - 1) ? dr : c.at(k + 1);
-            res[k] = cross7(wt, c.at(k), dn[j].at(k), up[j].at(k), cur[j].at(k), cur[j + 2].at(k), l, r);
+            res[k] = cross7(wt, c.at(k), dn.at(k), up.at(k), a.at(k), b.at(k), l, r);
           }
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
@@ -387,9 +383,14 @@ __global__ void __launch_bounds__(kTbThreads, 3)
               for (int k = 0; k < V; ++k) acc2.add(stored[k], c.at(k));
             }
           }
+          a = c;
+          c = b;
         }
         if (kRep & 2) acc2.flush(tot2);
       }
+      // every level-1 plane of the ring has been read before the next one is
+      // written over the oldest
+      tb_sync();
       ++n1;
     }
     if (s_abort) break;

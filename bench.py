@@ -794,6 +794,41 @@ def sample_iters(wl, updates=2e10):
     return max(1, int((0.6 * updates if "D" in wl else updates) // cells))
 
 
+def reference_gpu_path(wl):
+    """The reference's own GPU path on the same workload, beside its CPU arm:
+    ``runIterativeGPU`` (one kernel launch per step, 32 x 4 threads per block
+    as in the reference's test scripts, a device synchronisation after each
+    step; PSkelStencil.hpp:1046-1097). Two runs (the workload's iterations and
+    a tenth of them) give the per-step time of the step loop alone by their
+    difference; ``e2e`` is the reference's own GPU_time of the full run
+    (copies in and out included). Only the 2D workloads it runs as shipped
+    (Life u8, Jacobi f32)."""
+    import oracle
+    if wl["name"] not in ("life", "jacobi"):
+        return None
+    if not oracle.have_ref_gpu() or not Path("/dev/nvidiactl").exists():
+        return {"unavailable": "no GPU or oracle/_ref/pskel_ref_gpu not built"}
+    from pskel_gb300 import synth as S
+    x = make_inputs(wl)
+    full = wl["iters"]
+    short = max(2, full // 10)
+    runs = {}
+    for its in (short, full):
+        if wl["name"] == "life":
+            _, t = oracle.ref_gpu_life(x["in"], x["out"], its)
+        else:
+            _, t = oracle.ref_gpu_lin2d(x["in"], x["out"], S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, its)
+        runs[its] = t
+    cells = wl["W"] * wl["H"]
+    per_step = (runs[full]["gpu_time_s"] - runs[short]["gpu_time_s"]) / (full - short)
+    return {"impl": "runIterativeGPU (stencilTilingCU, one launch per step), blocks 32x4",
+            "value": round(cells / per_step / 1e9, 4), "unit": "GCells/s", "ms_per_iteration": round(per_step * 1e3, 4),
+            "e2e": round(cells * full / runs[full]["gpu_time_s"] / 1e9, 4),
+            "gpu_time_s": {str(k): round(v["gpu_time_s"], 6) for k, v in runs.items()},
+            "note": "value: the step loop alone (difference of the two runs); e2e: the reference's GPU_time of the "
+                    "full run, host copies included"}
+
+
 def run_reference_arm(args, wl, world, rank):
     if rank != 0:
         return None
@@ -825,7 +860,8 @@ def run_reference_arm(args, wl, world, rank):
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 4), "unit": "GCells/s", "cores": threads, "kind": kind,
                              "sample": sample},
-            "e2e": {"value": round(value, 4), "unit": "GCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(value, 4), "unit": "GCells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_path": reference_gpu_path(wl)}
 
 
 OTHERS = ["jacobi", "jacobi_bf16", "advect", "advect_bf16", "heat3d", "heat3d_bf16", "batch", "batch_bf16"]

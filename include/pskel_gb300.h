@@ -326,8 +326,10 @@ PSKEL_API pskel_status pskel_set_cost_model(pskel_mlp* m);
  * launches a kernel that waits on an mbarrier phase that never completes
  * (which = 0) or on a device flag that nothing sets (which = 1) for at most
  * `polls` polls (1..2^20), then records the timeout in the device error word
- * and returns. The next pskel_sync(stream) reports PSKEL_ERR_DEVICE (and
- * clears it); the context stays usable. */
+ * and returns; which = 2 launches the persistent Life kernel at pass 1 of a
+ * run whose pass 0 never ran, with a dependency-wait limit of `polls`, so its
+ * own wait runs out and its blocks stop. The next pskel_sync(stream) reports
+ * PSKEL_ERR_DEVICE (and clears it); the context stays usable. */
 PSKEL_API pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* stream);
 
 /* pskel_iterate3d without any allocation by the library. It has no

@@ -11,6 +11,9 @@ package, and only as the checker or the timed CPU baseline. The product
   ``tests/golden``.
 * ``ref_runner.cpp`` -> ``_ref/pskel_ref``: the reference's own
   ``Stencil2D/3D::runIterativeCPU`` built from its headers by ``make_ref.py``.
+* ``ref_runner_gpu.cu`` -> ``_ref/pskel_ref_gpu``: the reference's own
+  ``Stencil2D::runIterativeGPU`` (one kernel launch per step), the GPU path
+  the library is measured beside (``--impl reference`` and a GPU test).
 """
 from __future__ import annotations
 
@@ -26,6 +29,7 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libpskel_oracle.so"
 REF_BIN = HERE / "_ref" / "pskel_ref"
+REF_GPU_BIN = HERE / "_ref" / "pskel_ref_gpu"
 
 _lib = None
 
@@ -182,6 +186,55 @@ def ref_life(a_in, a_out, iters, threads=4):
         np.ascontiguousarray(a_out, dtype=np.uint8).tofile(d / "out")
         stdout = _run(["life", W, H, iters, threads, d / "in", d / "out", d / "res"], threads)
         return np.fromfile(d / "res", dtype=np.uint8).reshape(H, W), stdout
+
+
+def have_ref_gpu() -> bool:
+    return REF_GPU_BIN.exists()
+
+
+def _parse_gpu_run(stdout: str) -> dict:
+    """The timed call's lines: the reference's own ``GPU_time <s>`` print
+    (copies in and out plus the step loop, PSkelStencil.hpp:1067-1091) and the
+    runner's ``{"wall_s", "cell_updates"}`` (the whole call)."""
+    import json
+    lines = [ln for ln in stdout.splitlines() if ln.strip()]
+    info = json.loads(lines[-1])
+    gpu_times = [float(ln.split()[1]) for ln in lines if ln.startswith("GPU_time")]
+    info["gpu_time_s"] = gpu_times[-1]
+    return info
+
+
+def ref_gpu_life(a_in, a_out, iters, block=(32, 4)):
+    """The reference's ``runIterativeGPU`` on the Game of Life: (result, timing).
+    Only the interior is defined: the output array's ring comes from device
+    memory the reference never initialises (its copy of the output array to
+    the device is commented out, PSkelStencil.hpp:1071)."""
+    H, W = a_in.shape
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        np.ascontiguousarray(a_in, dtype=np.uint8).tofile(d / "in")
+        np.ascontiguousarray(a_out, dtype=np.uint8).tofile(d / "out")
+        out = subprocess.run([str(REF_GPU_BIN), "life", str(W), str(H), str(iters), str(block[0]), str(block[1]),
+                              str(d / "in"), str(d / "out"), str(d / "res")], check=True, capture_output=True,
+                             text=True)
+        return np.fromfile(d / "res", dtype=np.uint8).reshape(H, W), _parse_gpu_run(out.stdout)
+
+
+def ref_gpu_lin2d(a_in, a_out, offsets, weights, iters, block=(32, 4)):
+    """The reference's ``runIterativeGPU`` on a weighted float32 2D mask:
+    (result, timing); interior only, as for ``ref_gpu_life``. nvcc contracts
+    the weighted sum into FMAs, so the values differ from the CPU path's in
+    the last bits."""
+    H, W = a_in.shape
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        _write_mask(d / "m.txt", offsets, weights)
+        np.ascontiguousarray(a_in, dtype=np.float32).tofile(d / "in")
+        np.ascontiguousarray(a_out, dtype=np.float32).tofile(d / "out")
+        out = subprocess.run([str(REF_GPU_BIN), "lin2d", str(W), str(H), str(iters), str(block[0]), str(block[1]),
+                              str(d / "m.txt"), str(d / "in"), str(d / "out"), str(d / "res")], check=True,
+                             capture_output=True, text=True)
+        return np.fromfile(d / "res", dtype=np.float32).reshape(H, W), _parse_gpu_run(out.stdout)
 
 
 def ref_advect(a_in, a_out, u, v, iters, K, dt, inv_dx, dtype="f32", threads=4):

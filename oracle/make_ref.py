@@ -1,8 +1,9 @@
-"""Build recipe for ``oracle/_ref``: the reference's own ``runIterativeCPU``.
+"""Build recipe for ``oracle/_ref``: the reference's own ``runIterativeCPU``
+(and its ``runIterativeGPU``, to measure the library beside it).
 
 Test infrastructure only. The product never imports, links or runs anything
-under ``oracle/``; tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg
-of ``bench.py`` use it as the checker.
+under ``oracle/``; tests, ``__graft_entry__.smoke()`` and the CPU-baseline and
+reference legs of ``bench.py`` use it as the checker and the baseline.
 
 The reference (PSkel, header-only C++) does not compile for the CPU as shipped:
 ``PSkelArray.hpp`` defines three groups of CUDA-only members outside any
@@ -20,13 +21,17 @@ This script therefore:
      revision is refused instead of being patched blindly, and qualifies the
      two device accesses of lines 345 and 642 (``width``/``depth`` of a
      dependent base) with ``this->`` so the copy also compiles under nvcc with
-     ``PSKEL_CUDA`` (used only to show that user code compiles against it),
+     ``PSKEL_CUDA`` (to show that user code compiles against it, and for the
+     GPU runner below),
   3. writes two shim headers (``tbb/scalable_allocator.h`` over malloc/free and
      ``xmmintrin.h`` over posix_memalign, which also makes the build portable
      to aarch64 hosts),
   4. compiles ``oracle/ref_runner.cpp`` against the copy with
      ``g++ -O3 -ffp-contract=off -fopenmp -DPSKEL_OMP`` into
-     ``oracle/_ref/pskel_ref``.
+     ``oracle/_ref/pskel_ref``, and ``oracle/ref_runner_gpu.cu`` (the
+     reference's own ``runIterativeGPU``, measured beside the library) with
+     ``nvcc -O3 -DPSKEL_CUDA`` for sm_103a into ``oracle/_ref/pskel_ref_gpu``
+     when nvcc is present.
 
 Step 1-3 need the reference tree (the ``PSKEL_REFERENCE`` environment
 variable, else a ``reference`` directory beside this repository's root). Step 4 only needs ``oracle/_ref/src``,
@@ -46,6 +51,7 @@ OUT = HERE / "_ref"
 SRC = OUT / "src"
 SHIM = OUT / "shim"
 BIN = OUT / "pskel_ref"
+GPU_BIN = OUT / "pskel_ref_gpu"
 
 # sha256 of the reference PSkelArray.hpp the line ranges below were read from.
 ARRAY_HPP_SHA256 = "eee8c8e0c3e492be63452c199138c7b73d5ac7af7b0a2e8527e2e8d8c6d06fe6"
@@ -122,8 +128,17 @@ def compile_runner() -> Path:
     return BIN
 
 
+def gpu_runner_cmd() -> list[str]:
+    """nvcc command of ``pskel_ref_gpu``: the reference's GPU path as its own
+    build would compile it (``PSKEL_CUDA``, nvcc's default contraction)."""
+    return ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-O3", "-DPSKEL_CUDA",
+            "-DPSKEL_OMP", "-Xcompiler", "-fopenmp", "-include", "cstring", "-I", str(SHIM), "-I", str(SRC),
+            "-w", str(HERE / "ref_runner_gpu.cu"), "-o", str(GPU_BIN), "-lgomp"]
+
+
 def build(require: bool = False) -> Path | None:
-    """Prepare (when the reference tree is present) and compile ``pskel_ref``."""
+    """Prepare (when the reference tree is present) and compile ``pskel_ref``
+    and, when nvcc is on the path, ``pskel_ref_gpu`` (both at once)."""
     inc = reference_include()
     if inc is not None:
         prepare_overlay(inc)
@@ -131,7 +146,13 @@ def build(require: bool = False) -> Path | None:
         if require:
             raise RuntimeError("reference headers unavailable: no overlay copy in oracle/_ref/src")
         return None
-    return compile_runner()
+    gpu = subprocess.Popen(gpu_runner_cmd()) if shutil.which("nvcc") else None
+    try:
+        path = compile_runner()
+    finally:
+        if gpu is not None and gpu.wait() != 0:
+            print("oracle: pskel_ref_gpu did not compile; the reference GPU comparison is skipped", file=sys.stderr)
+    return path
 
 
 if __name__ == "__main__":

@@ -61,10 +61,12 @@ struct LifeWindow {
   long long start[kLifeMaxWindow + 1];
 };
 cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t s);
-// restart: clear the item counter first (the completion counts carry over)
+// restart: clear the item counter first (the completion counts carry over);
+// spin_limit: polls of a dependency wait before it latches kDevErrBarrier (0:
+// the library's limit; the bounded-wait self-test passes a short one)
 cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int ring, const LifeWindow& win, int q,
                                  int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s,
-                                 bool restart = true);
+                                 bool restart = true, unsigned spin_limit = 0);
 // Pack rows [row0, row1) (every cell checked to be 0/1) / unpack the interior
 // cells of rows [row0, row1).
 cudaError_t life_bits_pack_rows(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring,

@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
                                 uint32_t* __restrict__ planeX, uint32_t* __restrict__ planeY, int PW, int W, int H,
                                 int ring, int q, int r, int T, int TH, int tiles_x, int tiles_y,
                                 unsigned long long* next_item, unsigned* done, unsigned* err,
-                                const __grid_constant__ LifeWindow win) {
+                                const __grid_constant__ LifeWindow win, unsigned spin_limit) {
   using G = LifeGeo<R, NW>;
   extern __shared__ __align__(128) uint8_t lsm_raw[];
   uint32_t* win_src = reinterpret_cast<uint32_t*>(lsm_raw);
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
                 valid = 0;
                 break;
               }
-              if (++polls >= kLifeSpinLimit) {
+              if (++polls >= spin_limit) {
                 atomicOr(err, kDevErrBarrier);
                 valid = 0;
                 break;
@@ -571,7 +571,8 @@ cudaError_t life_bits_clear_sync(void* sync, int W, int H, int TH, cudaStream_t 
 
 cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int ring, const LifeWindow& win, int q,
                                  int r, int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s,
-                                 bool restart) {
+                                 bool restart, unsigned spin_limit) {
+  if (spin_limit == 0) spin_limit = kLifeSpinLimit;
   if (T < 1 || T > kLifeBitsMaxT || TH < 1 || TH > life_bits_max_tile_h(T)) return cudaErrorInvalidValue;
   const int PW = life_bits_words(W);
   const int tiles_x = life_bits_tiles_x(W);
@@ -594,7 +595,7 @@ cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int rin
   if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
   if (e != cudaSuccess) return e;
   life_kernel<<<ctas, LifeKernelGeo::kThreads, LifeKernelGeo::kSmemBytes, s>>>(
-      mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y, next, done, err, win);
+      mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y, next, done, err, win, spin_limit);
   return cudaGetLastError();
 }
 

@@ -1,11 +1,18 @@
 // A self-test of the bounded waits every kernel of the library relies on: a
 // kernel waits on an mbarrier phase that never completes, or on a device flag
-// that nothing sets, with a short poll limit. It gives up, records the timeout
-// in the device error word and returns, so the host reads PSKEL_ERR_DEVICE
-// from pskel_sync and the context stays usable. Nothing faults, traps or hangs.
+// that nothing sets, with a short poll limit; or the persistent Life kernel
+// itself is launched at pass 1 of a run whose pass 0 never ran, so the
+// dependency wait of its first item runs out. The wait gives up, records the
+// timeout in the device error word and returns (the Life kernel's other blocks
+// see the latched word and stop), so the host reads PSKEL_ERR_DEVICE from
+// pskel_sync and the context stays usable. Nothing faults, traps or hangs.
 #include "../../include/pskel_gb300.h"
 #include "capi_internal.h"
+#include <algorithm>
+#include <cstring>
+
 #include "common.cuh"
+#include "kernels.h"
 
 namespace pskel {
 namespace {
@@ -45,12 +52,34 @@ extern "C" {
 
 pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* stream) {
   clear_error();
-  if ((which != 0 && which != 1) || polls == 0 || polls > (1u << 20))
-    return fail(PSKEL_ERR_INVALID, "selftest: which must be 0 or 1 and polls in 1..2^20");
+  if (which < 0 || which > 2 || polls == 0 || polls > (1u << 20))
+    return fail(PSKEL_ERR_INVALID, "selftest: which must be 0, 1 or 2 and polls in 1..2^20");
   DeviceContext* c = nullptr;
   if (pskel_status s = get_context(&c)) return s;
-  selftest_wait_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(which, polls, c->err);
-  const cudaError_t e = cudaGetLastError();
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (which < 2) {
+    selftest_wait_kernel<<<1, 32, 0, s>>>(which, polls, c->err);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PSKEL_OK : cuda_fail(e, "selftest launch");
+  }
+  // the Life kernel on a 512 x 512 grid of zeros, launched for pass 1 only with
+  // cleared completion counts: every item waits for pass 0, which never ran
+  const int W = 512, H = 512, T = 3;
+  const int TH = life_bits_max_tile_h(T);
+  const size_t plane = static_cast<size_t>(life_bits_words(W)) * H;
+  if (pskel_status q = ensure_buffer(c->life_bits, 2 * plane * sizeof(uint32_t))) return q;
+  if (pskel_status q = ensure_buffer(c->life_sync, life_bits_sync_bytes(W, H, TH))) return q;
+  uint32_t* X = static_cast<uint32_t*>(c->life_bits.ptr);
+  cudaError_t e = cudaMemsetAsync(X, 0, 2 * plane * sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = life_bits_clear_sync(c->life_sync.ptr, W, H, TH, s);
+  if (e != cudaSuccess) return cuda_fail(e, "selftest set-up");
+  LifeWindow win;
+  memset(&win, 0, sizeof(win));
+  win.pass0 = 1;
+  win.np = 1;
+  const int ctas = static_cast<int>(std::min<int64_t>(life_bits_tiles(W, H, TH),
+                                                      static_cast<int64_t>(life_bits_persistent_ctas_per_sm()) * c->sms));
+  e = life_bits_run_window(X, X + plane, W, H, 1, win, 1, 0, T, TH, ctas, c->life_sync.ptr, c->err, s, true, polls);
   return e == cudaSuccess ? PSKEL_OK : cuda_fail(e, "selftest launch");
 }
 

@@ -25,6 +25,9 @@ def test_reference_arm_line():
     assert "whole workload" in cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": "GCells/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    # the reference's own GPU path beside it: measured on a GPU node, marked unavailable here
+    gp = line["gpu_path"]
+    assert ("unavailable" in gp) if not Path("/dev/nvidiactl").exists() else gp["value"] > 0
 
 
 def test_reference_arm_maps_no_library_of_ours():

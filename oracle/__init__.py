@@ -206,9 +206,10 @@ def _parse_gpu_run(stdout: str) -> dict:
 
 def ref_gpu_life(a_in, a_out, iters, block=(32, 4)):
     """The reference's ``runIterativeGPU`` on the Game of Life: (result, timing).
-    Only the interior is defined: the output array's ring comes from device
-    memory the reference never initialises (its copy of the output array to
-    the device is commented out, PSkelStencil.hpp:1071)."""
+    The output array is never copied to the device (PSkelStencil.hpp:1071), so
+    from the second step on the ring read comes from a fresh device
+    allocation: cells within ``iters`` of the edge may differ from the CPU
+    path's."""
     H, W = a_in.shape
     with tempfile.TemporaryDirectory() as d:
         d = Path(d)
@@ -222,9 +223,9 @@ def ref_gpu_life(a_in, a_out, iters, block=(32, 4)):
 
 def ref_gpu_lin2d(a_in, a_out, offsets, weights, iters, block=(32, 4)):
     """The reference's ``runIterativeGPU`` on a weighted float32 2D mask:
-    (result, timing); interior only, as for ``ref_gpu_life``. nvcc contracts
-    the weighted sum into FMAs, so the values differ from the CPU path's in
-    the last bits."""
+    (result, timing), with the ring caveat of ``ref_gpu_life``. nvcc contracts
+    the weighted sum into FMAs, which round like the separate product and sum
+    only when the products are exact (power-of-two weights)."""
     H, W = a_in.shape
     with tempfile.TemporaryDirectory() as d:
         d = Path(d)

@@ -47,6 +47,7 @@ struct BatchSeg {
 struct BatchParams {
   float wt[9];
   unsigned* err;
+  uint32_t fuse_guard;  // always 0: the kernel forms -0.0f from it at run time (neg_zero2)
 };
 
 constexpr unsigned kBatchSpinLimit = 1u << 24;  // polls of a completion counter (with a short sleep each)
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     g.K = g.dt = g.inv_dx = 0.0f;
     g.u = g.v = nullptr;
     TS* dst = static_cast<TS*>(fwd ? G.out : G.in);
-    fast2d_run_tile<TS, OpK, S>(buf0, buf1, dst, g, gy0, gx0, ring_tile, wt);
+    fast2d_run_tile<TS, OpK, S>(buf0, buf1, dst, g, gy0, gx0, ring_tile, wt, neg_zero2(bp.fuse_guard));
     __syncthreads();
     if (tid == 0) {
       __threadfence();

@@ -174,4 +174,74 @@ struct Vec16 {
   __device__ __forceinline__ void fill(uint32_t h) { r[0] = r[1] = r[2] = r[3] = h; }
 };
 
+// Paired fp32 arithmetic (Blackwell's add/sub/fma.f32x2): two lanes per
+// instruction, each rounded to nearest like the scalar .rn forms, so every lane
+// matches the reference's unfused scalar arithmetic bit for bit -- provided no
+// product is fused into the sum it feeds. ptxas does fuse a paired product
+// (mul.rn.f32x2, or fma.rn.f32x2 with a constant -0 addend) into a paired sum,
+// .rn and -fmad=false notwithstanding, so a product is written as
+// fma(a, b, z) with z = (-0, -0) formed at run time from a kernel parameter
+// (neg_zero2): fma(a, b, -0) rounds exactly like a*b, signed zeros included,
+// and fma(a, b, z) + c is no single multiply-add.
+__device__ __forceinline__ unsigned long long f2_bits(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_from(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+// guard: a kernel parameter that is always 0 (the zero-initialised
+// fuse_guard field of the launch parameters)
+__device__ __forceinline__ float2 neg_zero2(uint32_t guard) {
+  const float z = __uint_as_float(guard ^ 0x80000000u);
+  return make_float2(z, z);
+}
+__device__ __forceinline__ float2 fmul2_rn(float2 a, float2 b, float2 nz) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(nz)));
+  return f2_from(d);
+}
+__device__ __forceinline__ float2 fadd2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(d);
+}
+__device__ __forceinline__ float2 fsub2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(d);
+}
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// The 7-point weighted sum of the reference's order (centre, h-1, h+1, w-1,
+// w+1, d-1, d+1; products and sums unfused) for the V cells of one vector row,
+// two neighbouring cells per instruction: fmul2_rn / fadd2_rn round each lane
+// exactly as __fmul_rn / __fadd_rn, so every cell gets the scalar result. wt2[n] holds (wt[n], wt[n]). The d-neighbour products are formed
+// one lane at a time: the pair (c[k-1], c[k]) straddles two register pairs,
+// and two scalar products cost less than gathering it.
+template <class Vt>
+__device__ __forceinline__ void cross7_row(const float* wt, const float2* wt2, float2 nz, const Vt& c, const Vt& dn,
+                                           const Vt& up, const Vt& a, const Vt& b, float dl, float dr,
+                                           float (&res)[Vt::V]) {
+  constexpr int V = Vt::V;
+#pragma unroll
+  for (int k = 0; k < V; k += 2) {
+    const float c0 = c.at(k), c1 = c.at(k + 1);
+    const float l0 = k == 0 ? dl : c.at(k - 1);
+    const float r1 = k + 2 == V ? dr : c.at(k + 2);
+    float2 acc = fmul2_rn(wt2[0], make_float2(c0, c1), nz);
+    acc = fadd2_rn(acc, fmul2_rn(wt2[1], make_float2(dn.at(k), dn.at(k + 1)), nz));
+    acc = fadd2_rn(acc, fmul2_rn(wt2[2], make_float2(up.at(k), up.at(k + 1)), nz));
+    acc = fadd2_rn(acc, fmul2_rn(wt2[3], make_float2(a.at(k), a.at(k + 1)), nz));
+    acc = fadd2_rn(acc, fmul2_rn(wt2[4], make_float2(b.at(k), b.at(k + 1)), nz));
+    acc = fadd2_rn(acc, make_float2(__fmul_rn(wt[5], l0), __fmul_rn(wt[5], c0)));
+    acc = fadd2_rn(acc, make_float2(__fmul_rn(wt[6], c1), __fmul_rn(wt[6], r1)));
+    res[k] = acc.x;
+    res[k + 1] = acc.y;
+  }
+}
+
 }  // namespace pskel

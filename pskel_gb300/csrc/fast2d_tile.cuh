@@ -126,6 +126,26 @@ __device__ __forceinline__ float advect_cell(float cc, float n_, float e_, float
   return __fadd_rn(__fadd_rn(cc, cond), __fmul_rn(temp_wind, dt));
 }
 
+// advect_cell for two horizontally neighbouring cells at once (x in lane .x,
+// x+1 in lane .y), the same operations in the same order per lane, two cells
+// per instruction where the operands come in register pairs. The east and
+// west pairs straddle two register pairs (east of x is the centre of x+1), so
+// the first two sums of the neighbourhood take one instruction per lane. nz:
+// neg_zero2 of the launch.
+__device__ __forceinline__ float2 advect_pair(float2 cc, float2 n_, float2 e_, float2 w_, float2 s_, float2 xw,
+                                              float2 yw, float K, float dt, float inv_dx, float2 nz) {
+  const float2 new_ = make_float2(__fadd_rn(__fadd_rn(n_.x, e_.x), w_.x), __fadd_rn(__fadd_rn(n_.y, e_.y), w_.y));
+  const float2 sum = fsub2_rn(fmul2_rn(dup2(4.0f), cc, nz), fadd2_rn(new_, s_));
+  const float2 cvy = make_float2((yw.x > 0.0f) ? yw.x : -yw.x, (yw.y > 0.0f) ? yw.y : -yw.y);
+  const float2 ncvx = make_float2((xw.x > 0.0f) ? -xw.x : xw.x, (xw.y > 0.0f) ? -xw.y : xw.y);  // -cvx
+  const float2 nbx = make_float2((xw.x > 0.0f) ? e_.x : w_.x, (xw.y > 0.0f) ? e_.y : w_.y);
+  const float2 nby = make_float2((yw.x > 0.0f) ? s_.x : n_.x, (yw.y > 0.0f) ? s_.y : n_.y);
+  const float2 temp_wind = fsub2_rn(fmul2_rn(ncvx, fmul2_rn(fsub2_rn(cc, nbx), dup2(inv_dx), nz), nz),
+                                    fmul2_rn(cvy, fmul2_rn(fsub2_rn(cc, nby), dup2(inv_dx), nz), nz));
+  const float2 cond = fmul2_rn(fmul2_rn(dup2(-K), fmul2_rn(sum, dup2(0.25f), nz), nz), dup2(dt), nz);
+  return fadd2_rn(fadd2_rn(cc, cond), fmul2_rn(temp_wind, dup2(dt), nz));
+}
+
 // Geometry and op parameters of one tile's grid (passed in registers).
 struct TileGeom {
   int W, H, ring, steps;
@@ -141,7 +161,7 @@ struct TileGeom {
 // writes the core's interior cells to dst. All threads of the block call it.
 template <class TS, int OpK, int S>
 __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, const TileGeom& g, int gy0, int gx0,
-                                                bool ring_tile, const float* wt) {
+                                                bool ring_tile, const float* wt, float2 nz) {
   constexpr int N = Vec<TS>::N;
   constexpr int LW = 32 * N;
   constexpr bool kAdvect = (OpK == 3);
@@ -154,6 +174,9 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
   const TS* wu = static_cast<const TS*>(g.u);
   const TS* wv = static_cast<const TS*>(g.v);
   const int gxv = gx0 + x0;
+  float2 wt2[shp.n > 0 ? shp.n : 1];
+#pragma unroll
+  for (int n = 0; n < shp.n; ++n) wt2[n] = make_float2(wt[n], wt[n]);
   for (int s = 1; s <= g.steps; ++s) {
     const TS* in = ((s & 1) ? sbuf : pbuf);
     TS* out = ((s & 1) ? pbuf : sbuf);
@@ -181,22 +204,38 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
       const int y = yb - 1 + k;
       if (y < s || y >= LH - s) continue;
       float res[N];
+      // two neighbouring cells per instruction (cells c, c+1: lanes .x, .y)
       if constexpr (!kAdvect) {
 #pragma unroll
-        for (int c = 0; c < N; ++c) {
-          float acc = __fmul_rn(wt[0], win[k + shp.dh[0]][1 + c + shp.dw[0]]);
+        for (int c = 0; c < N; c += 2) {
+          float2 acc;
 #pragma unroll
-          for (int n = 1; n < shp.n; ++n) acc = __fadd_rn(acc, __fmul_rn(wt[n], win[k + shp.dh[n]][1 + c + shp.dw[n]]));
-          res[c] = acc;
+          for (int n = 0; n < shp.n; ++n) {
+            const int dh = shp.dh[n], dw = shp.dw[n];
+            // a row neighbour (dw != 0) straddles two register pairs: one
+            // product per lane
+            const float2 t = (dw == 0) ? fmul2_rn(wt2[n], make_float2(win[k + dh][1 + c], win[k + dh][2 + c]), nz)
+                                       : make_float2(__fmul_rn(wt[n], win[k + dh][1 + c + dw]),
+                                                     __fmul_rn(wt[n], win[k + dh][2 + c + dw]));
+            acc = (n == 0) ? t : fadd2_rn(acc, t);
+          }
+          res[c] = acc.x;
+          res[c + 1] = acc.y;
         }
       } else {
         float uu[N], vv[N];
         ld_wind(wu, g.pitch, gy0 + y, gxv, g.W, g.H, uu);
         ld_wind(wv, g.pitch, gy0 + y, gxv, g.W, g.H, vv);
 #pragma unroll
-        for (int c = 0; c < N; ++c)
-          res[c] = advect_cell(win[k][1 + c], win[k - 1][1 + c], win[k][2 + c], win[k][c], win[k + 1][1 + c], uu[c],
-                               vv[c], g.K, g.dt, g.inv_dx);
+        for (int c = 0; c < N; c += 2) {
+          const float2 r2 = advect_pair(
+              make_float2(win[k][1 + c], win[k][2 + c]), make_float2(win[k - 1][1 + c], win[k - 1][2 + c]),
+              make_float2(win[k][2 + c], win[k][3 + c]), make_float2(win[k][c], win[k][1 + c]),
+              make_float2(win[k + 1][1 + c], win[k + 1][2 + c]), make_float2(uu[c], uu[c + 1]),
+              make_float2(vv[c], vv[c + 1]), g.K, g.dt, g.inv_dx, nz);
+          res[c] = r2.x;
+          res[c + 1] = r2.y;
+        }
       }
       TS* o = out + y * LW + x0;
       if (ring_tile) {

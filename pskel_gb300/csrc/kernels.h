@@ -104,6 +104,7 @@ struct Stencil2DParams {
   const void* u;
   const void* v;
   unsigned* err;
+  uint32_t fuse_guard;  // always 0: the kernels form -0.0f from it at run time (neg_zero2)
 };
 
 struct Stencil2DGeom {
@@ -197,6 +198,7 @@ struct Stencil3DParams {
   double* partials;    // scratch: steps x ctas fp64 partial sums
   double* residuals;   // device: one norm per reported step
   int hbeg, hend;      // streaming 7-point kernel: planes [hbeg, hend) (hend 0: all)
+  uint32_t fuse_guard;  // always 0: the kernels form -0.0f from it at run time (neg_zero2)
 };
 
 // The 7-point cross, two steps per launch (stream3d_tb.cu): the one-step

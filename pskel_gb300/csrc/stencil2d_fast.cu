@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     g.inv_dx = p.inv_dx;
     g.u = p.u;
     g.v = p.v;
-    fast2d_run_tile<TS, OpK, S>(buf(bs), buf(bp), dst, g, gy0, gx0, ring_tile, wt);
+    fast2d_run_tile<TS, OpK, S>(buf(bs), buf(bp), dst, g, gy0, gx0, ring_tile, wt, neg_zero2(p.fuse_guard));
     __syncthreads();
   }
 }
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     g.u = p.u;
     g.v = p.v;
     TS* dst = static_cast<TS*>(fwd ? p.dst : const_cast<void*>(p.src));
-    fast2d_run_tile<TS, OpK, S>(buf0, buf1, dst, g, gy0, gx0, ring_tile, wt);
+    fast2d_run_tile<TS, OpK, S>(buf0, buf1, dst, g, gy0, gx0, ring_tile, wt, neg_zero2(p.fuse_guard));
     __threadfence();
     __syncthreads();
     if (tid == 0) {

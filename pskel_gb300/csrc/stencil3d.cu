@@ -454,6 +454,10 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
   const int o_er = r0 * kS3RowBytes + 33 * 16;                                  // d0+32V
   SqDiffAcc acc_res;
   double acc_total = 0.0;
+  float2 wt2[5];
+#pragma unroll
+  for (int n = 0; n < 5; ++n) wt2[n] = make_float2(p.wt[n], p.wt[n]);
+  const float2 nz = neg_zero2(p.fuse_guard);
   auto ld = [&](int slot, int off, Vt& v) {
     const uint4 x = *reinterpret_cast<const uint4*>(sbase + slot * kS3PlaneBytes + off);
     v.r[0] = x.x;
@@ -545,44 +549,27 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
         if (lane == 31) dr = er[j];
         const Vt& a = (j == 0) ? wm : cur[j > 0 ? j - 1 : 0];
         const Vt& b = (j == kRW - 1) ? wp : cur[j < kRW - 1 ? j + 1 : 0];
+        float res[V], stored[V];
+        cross7_row(p.wt, wt2, nz, cur[j], dn[j], up[j], a, b, dl, dr, res);
         uint32_t o[4];
-#pragma unroll
-        for (int g = 0; g < V / 4; ++g) {
-          float res[4];
+        if constexpr (sizeof(TS) == 4) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const int c = 4 * g + k;
-            const float l = (c == 0) ? dl : cur[j].at(c - 1);
-            const float r = (c == V - 1) ? dr : cur[j].at(c + 1);
-            float acc = __fmul_rn(p.wt[0], cur[j].at(c));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[1], dn[j].at(c)));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[2], up[j].at(c)));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[3], a.at(c)));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[4], b.at(c)));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[5], l));
-            acc = __fadd_rn(acc, __fmul_rn(p.wt[6], r));
-            res[k] = acc;
+            o[k] = __float_as_uint(res[k]);
+            stored[k] = res[k];
           }
-          float stored[4];
-          if constexpr (sizeof(TS) == 4) {
+        } else {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              o[k] = __float_as_uint(res[k]);
-              stored[k] = res[k];
-            }
-          } else {
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              const __nv_bfloat162 bb = __floats2bfloat162_rn(res[2 * k], res[2 * k + 1]);
-              o[2 * g + k] = *reinterpret_cast<const uint32_t*>(&bb);
-              stored[2 * k] = __uint_as_float(o[2 * g + k] << 16);
-              stored[2 * k + 1] = __uint_as_float(o[2 * g + k] & 0xFFFF0000u);
-            }
+          for (int k = 0; k < 4; ++k) {
+            const __nv_bfloat162 bb = __floats2bfloat162_rn(res[2 * k], res[2 * k + 1]);
+            o[k] = *reinterpret_cast<const uint32_t*>(&bb);
+            stored[2 * k] = __uint_as_float(o[k] << 16);
+            stored[2 * k + 1] = __uint_as_float(o[k] & 0xFFFF0000u);
           }
-          if (kReport && row_ok[j]) {
+        }
+        if (kReport && row_ok[j]) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) acc_res.add(stored[k], cur[j].at(4 * g + k));
-          }
+          for (int k = 0; k < V; ++k) acc_res.add(stored[k], cur[j].at(k));
         }
         if (row_ok[j]) *reinterpret_cast<uint4*>(out + j * D) = make_uint4(o[0], o[1], o[2], o[3]);
       }

@@ -12,7 +12,7 @@
 namespace pskel {
 namespace {
 
-using fast2d::advect_cell;
+using fast2d::advect_pair;
 using fast2d::shape_of;
 
 // Rows are staged by TMA. A persistent block owns work items of 32 16-byte
@@ -70,6 +70,10 @@ __global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __gri
   }
   __syncthreads();
   const int W = p.W, H = p.H, ring = p.ring;
+  float2 wt2[kTerms > 0 ? kTerms : 1];
+#pragma unroll
+  for (int n = 0; n < kTerms; ++n) wt2[n] = make_float2(p.wt[n], p.wt[n]);
+  const float2 nz = neg_zero2(p.fuse_guard);
   const int strips = (W + 32 * V - 1) / (32 * V);
   const int64_t items = static_cast<int64_t>(strips) * p.tiles_y;
   // rows of an item that are written: [hs, he)
@@ -196,23 +200,30 @@ __global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __gri
       for (int j = 0; j < kR2RW; ++j) {
         const int r = rbase + j;
         if (!(r < he && c_ok)) continue;
+        // two neighbouring cells per instruction (cells kk, kk+1: lanes .x, .y)
         float res[V];
 #pragma unroll
-        for (int kk = 0; kk < V; ++kk) {
+        for (int kk = 0; kk < V; kk += 2) {
+          auto pr = [&](int q, int k0) { return make_float2(val(q, k0), val(q, k0 + 1)); };
+          float2 r2;
           if constexpr (kAdvect) {
-            res[kk] = advect_cell(rows[j + 1].at(kk), rows[j].at(kk), val(j + 1, kk + 1), val(j + 1, kk - 1),
-                                  rows[j + 2].at(kk), uu[j].at(kk), vv[j].at(kk), p.K, p.dt, p.inv_dx);
+            r2 = advect_pair(pr(j + 1, kk), pr(j, kk), pr(j + 1, kk + 1), pr(j + 1, kk - 1), pr(j + 2, kk),
+                             make_float2(uu[j].at(kk), uu[j].at(kk + 1)), make_float2(vv[j].at(kk), vv[j].at(kk + 1)),
+                             p.K, p.dt, p.inv_dx, nz);
           } else {
-            float acc = 0.0f;
 #pragma unroll
             for (int n = 0; n < kTerms; ++n) {
               const int dh = shape_of<kShape>().dh[n], dw = shape_of<kShape>().dw[n];
-              const float x = val(j + 1 + dh, kk + dw);
-              const float t = __fmul_rn(p.wt[n], x);
-              acc = (n == 0) ? t : __fadd_rn(acc, t);
+              // a row neighbour (dw != 0) straddles two register pairs: one
+              // product per lane
+              const float2 t = (dw == 0) ? fmul2_rn(wt2[n], pr(j + 1 + dh, kk), nz)
+                                         : make_float2(__fmul_rn(p.wt[n], val(j + 1 + dh, kk + dw)),
+                                                       __fmul_rn(p.wt[n], val(j + 1 + dh, kk + 1 + dw)));
+              r2 = (n == 0) ? t : fadd2_rn(r2, t);
             }
-            res[kk] = acc;
           }
+          res[kk] = r2.x;
+          res[kk + 1] = r2.y;
         }
         TS* o = dst + (static_cast<int64_t>(r) * pitch + c);
         if (full_vec) {

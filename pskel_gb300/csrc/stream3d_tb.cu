@@ -22,7 +22,8 @@
 // three level-1 slots. Every wait is bounded.
 //
 // Arithmetic: the reference's order (centre, h-1, h+1, w-1, w+1, d-1, d+1),
-// __fmul_rn / __fadd_rn, no contraction: bit-identical to two launches of the
+// __fmul_rn / __fadd_rn (two cells per instruction in the vector rows,
+// cross7_row), no contraction: bit-identical to two launches of the
 // one-step kernel.
 #include <algorithm>
 #include <cstring>
@@ -187,6 +188,10 @@ __global__ void __launch_bounds__(kTbThreads, 3)
   float wt[7];
 #pragma unroll
   for (int n = 0; n < 7; ++n) wt[n] = p.wt[n];
+  float2 wt2[5];
+#pragma unroll
+  for (int n = 0; n < 5; ++n) wt2[n] = make_float2(wt[n], wt[n]);
+  const float2 nz = neg_zero2(p.fuse_guard);
   TS* __restrict__ dst = static_cast<TS*>(p.dst);
   const int64_t plane = static_cast<int64_t>(W) * D;
   const bool edge = warp == kTbEdge;
@@ -250,12 +255,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           if (lane == 0) dl = el;
           if (lane == 31) dr = er;
           float res[V], stored[V];
-#pragma unroll
-          for (int k = 0; k < V; ++k) {
-            const float l = (k == 0) ? dl : c.at(k - 1);
-            const float r = (k == V - 1) ? dr : c.at(k + 1);
-            res[k] = cross7(wt, c.at(k), dn.at(k), up.at(k), a.at(k), b.at(k), l, r);
-          }
+          cross7_row(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
           const bool valid = plane_in && d_ok && w < W;
@@ -298,12 +298,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           if (lane == 0) dl = el;
           if (lane == 31) dr = er;
           float res[V], stored[V];
-#pragma unroll
-          for (int k = 0; k < V; ++k) {
-            const float l = (k == 0) ? dl : c.at(k - 1);
-            const float rr = (k == V - 1) ? dr : c.at(k + 1);
-            res[k] = cross7(wt, c.at(k), dn.at(k), up.at(k), a.at(k), b.at(k), l, rr);
-          }
+          cross7_row(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
           if (!(plane_in && d_ok && w >= 0 && w < W)) o[0] = o[1] = o[2] = o[3] = hraw;
@@ -368,12 +363,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           if (lane == 0) dl = el;
           if (lane == 31) dr = er;
           float res[V], stored[V];
-#pragma unroll
-          for (int k = 0; k < V; ++k) {
-            const float l = (k == 0) ? dl : c.at(k - 1);
-            const float r = (k == V - 1) ? dr : c.at(k + 1);
-            res[k] = cross7(wt, c.at(k), dn.at(k), up.at(k), a.at(k), b.at(k), l, r);
-          }
+          cross7_row(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
           if (d_ok && w0 + rb + j < W) {

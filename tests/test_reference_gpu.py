@@ -4,11 +4,14 @@ PSkelStencil.hpp:1046-1097, :572-652, :1764-1792), compiled from its headers
 by ``oracle/make_ref.py`` into ``oracle/_ref/pskel_ref_gpu`` and run beside the
 library as the plain-GPU comparator.
 
-Its interior agrees with the reference's CPU path (the oracle) bit for bit on
-the Game of Life; on a float mask nvcc's contraction into FMAs moves the last
-bits, so the check there is a tolerance. Its ring is not defined (the output
-array is never copied to the device, PSkelStencil.hpp:1071), so only the
-interior is compared. The timings are printed as ``REF-GPU`` lines."""
+Its ring is not the CPU path's: the output array is never copied to the
+device (PSkelStencil.hpp:1071), so from the second step on the ring read is
+whatever the fresh device allocation holds, and the difference moves inward
+one cell per step. Cells farther than ``iters`` from the edge agree with the
+reference's CPU path (the oracle) bit for bit on the Game of Life, and on the
+Jacobi mask (weights 0.25: a contracted multiply-add rounds like the separate
+product and sum); the first step agrees everywhere inside the ring. The
+timings are printed as ``REF-GPU`` lines."""
 from __future__ import annotations
 
 import numpy as np
@@ -29,20 +32,23 @@ def ref_gpu(cuda):
     return oracle
 
 
-@pytest.mark.parametrize("W,H,iters", [(1000, 777, 7), (1024, 1024, 8), (131, 67, 1)])
-def test_reference_gpu_life_interior_matches_oracle(ref_gpu, oracle_mod, W, H, iters):
+def core(x, m):
+    return x[m:-m, m:-m]
+
+
+@pytest.mark.parametrize("W,H,iters", [(1000, 777, 7), (1024, 1024, 8), (131, 67, 1), (131, 67, 2)])
+def test_reference_gpu_life_matches_oracle_away_from_ring(ref_gpu, oracle_mod, W, H, iters):
     a, b = S.life(W, H, seed=iters)
     got, t = ref_gpu.ref_gpu_life(a, b, iters)
     want = oracle_mod.life(a, b, iters)
-    assert np.array_equal(got[1:-1, 1:-1], want[1:-1, 1:-1])
+    assert np.array_equal(core(got, iters), core(want, iters))
     print("REF-GPU life", W, H, iters, t)
 
 
 @pytest.mark.parametrize("W,H,iters", [(300, 200, 5), (1024, 1024, 6)])
-def test_reference_gpu_jacobi_interior_close_to_oracle(ref_gpu, oracle_mod, W, H, iters):
+def test_reference_gpu_jacobi_matches_oracle_away_from_ring(ref_gpu, oracle_mod, W, H, iters):
     a, b = S.jacobi2d(W, H, seed=iters)
     got, t = ref_gpu.ref_gpu_lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters)
     want = oracle_mod.lin2d(a, b, S.JACOBI4_OFFSETS, S.JACOBI4_WEIGHTS, iters)
-    # a few ulp of contraction per step; Jacobi averages, so the difference stays small
-    np.testing.assert_allclose(got[1:-1, 1:-1], want[1:-1, 1:-1], rtol=1e-5, atol=1e-6)
+    assert np.array_equal(core(got, iters).view(np.uint32), core(want, iters).view(np.uint32))
     print("REF-GPU jacobi", W, H, iters, t)

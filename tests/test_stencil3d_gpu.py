@@ -100,6 +100,27 @@ def test_heat3d_two_step_streaming(cuda, oracle_mod, dtype, W, H, D, th, ctas, h
     np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
 
 
+# weights whose products round: a product fused with the following sum into
+# one multiply-add would change the last bit (the heat weights 1/4, 1/8 are
+# exact, so a fused and an unfused product agree there)
+INEXACT7 = [0.31, 0.07, 0.11, 0.13, 0.17, 0.09, 0.12]
+
+
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("T", [1, 2])
+@pytest.mark.parametrize("halo", [0.0, 0.5])
+@pytest.mark.parametrize("W,H,D", [(70, 37, 264), (17, 50, 40)])
+def test_cross7_inexact_weights(cuda, oracle_mod, dtype, T, halo, W, H, D):
+    keep = P._Keep()
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.HEAT7_OFFSETS, INEXACT7, halo=halo, keep=keep)
+    a, b = grids(W, H, D, W + T, dtype)
+    sch = dict(time_steps=T, tile_w=0, tile_h=0, tile_d=0, ctas=0)
+    got, res = run3d(cuda, st, a, b, 9, sched=sch, every=3, dtype=dtype)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, INEXACT7, 9, halo=halo, dtype=dtype, every=3)
+    assert np.array_equal(bits(got), bits(want))
+    np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
+
+
 @pytest.mark.parametrize("T,tw,td,th", [(1, 0, 0, 0), (2, 16, 32, 0), (3, 8, 16, 5), (4, 32, 64, 7), (8, 8, 8, 0),
                                         (2, 0, 0, 1), (3, 16, 16, 13)])
 def test_heat3d_schedules(cuda, oracle_mod, T, tw, td, th):

@@ -217,30 +217,49 @@ __device__ __forceinline__ float2 fsub2_rn(float2 a, float2 b) {
 __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
 
 // The 7-point weighted sum of the reference's order (centre, h-1, h+1, w-1,
-// w+1, d-1, d+1; products and sums unfused) for the V cells of one vector row,
-// two neighbouring cells per instruction: fmul2_rn / fadd2_rn round each lane
-// exactly as __fmul_rn / __fadd_rn, so every cell gets the scalar result. wt2[n] holds (wt[n], wt[n]). The d-neighbour products are formed
-// one lane at a time: the pair (c[k-1], c[k]) straddles two register pairs,
-// and two scalar products cost less than gathering it.
-template <class Vt>
+// w+1, d-1, d+1; products and sums unfused) for the V cells of one vector row.
+// kPaired: two neighbouring cells per instruction (fmul2_rn / fadd2_rn round
+// each lane exactly as __fmul_rn / __fadd_rn, so every cell gets the scalar
+// result); wt2[n] holds (wt[n], wt[n]), nz is neg_zero2 of the launch. The
+// d-neighbour products are formed one lane at a time: the pair (c[k-1], c[k])
+// straddles two register pairs, and two scalar products cost less than
+// gathering it. Without kPaired, one cell per instruction (the fp32 one-step
+// kernel, bound by HBM, measured faster so: 788 against 732 GCells/s).
+template <bool kPaired, class Vt>
 __device__ __forceinline__ void cross7_row(const float* wt, const float2* wt2, float2 nz, const Vt& c, const Vt& dn,
                                            const Vt& up, const Vt& a, const Vt& b, float dl, float dr,
                                            float (&res)[Vt::V]) {
   constexpr int V = Vt::V;
+  if constexpr (kPaired) {
 #pragma unroll
-  for (int k = 0; k < V; k += 2) {
-    const float c0 = c.at(k), c1 = c.at(k + 1);
-    const float l0 = k == 0 ? dl : c.at(k - 1);
-    const float r1 = k + 2 == V ? dr : c.at(k + 2);
-    float2 acc = fmul2_rn(wt2[0], make_float2(c0, c1), nz);
-    acc = fadd2_rn(acc, fmul2_rn(wt2[1], make_float2(dn.at(k), dn.at(k + 1)), nz));
-    acc = fadd2_rn(acc, fmul2_rn(wt2[2], make_float2(up.at(k), up.at(k + 1)), nz));
-    acc = fadd2_rn(acc, fmul2_rn(wt2[3], make_float2(a.at(k), a.at(k + 1)), nz));
-    acc = fadd2_rn(acc, fmul2_rn(wt2[4], make_float2(b.at(k), b.at(k + 1)), nz));
-    acc = fadd2_rn(acc, make_float2(__fmul_rn(wt[5], l0), __fmul_rn(wt[5], c0)));
-    acc = fadd2_rn(acc, make_float2(__fmul_rn(wt[6], c1), __fmul_rn(wt[6], r1)));
-    res[k] = acc.x;
-    res[k + 1] = acc.y;
+    for (int k = 0; k < V; k += 2) {
+      const float c0 = c.at(k), c1 = c.at(k + 1);
+      const float l0 = k == 0 ? dl : c.at(k - 1);
+      const float r1 = k + 2 == V ? dr : c.at(k + 2);
+      float2 acc = fmul2_rn(wt2[0], make_float2(c0, c1), nz);
+      acc = fadd2_rn(acc, fmul2_rn(wt2[1], make_float2(dn.at(k), dn.at(k + 1)), nz));
+      acc = fadd2_rn(acc, fmul2_rn(wt2[2], make_float2(up.at(k), up.at(k + 1)), nz));
+      acc = fadd2_rn(acc, fmul2_rn(wt2[3], make_float2(a.at(k), a.at(k + 1)), nz));
+      acc = fadd2_rn(acc, fmul2_rn(wt2[4], make_float2(b.at(k), b.at(k + 1)), nz));
+      acc = fadd2_rn(acc, make_float2(__fmul_rn(wt[5], l0), __fmul_rn(wt[5], c0)));
+      acc = fadd2_rn(acc, make_float2(__fmul_rn(wt[6], c1), __fmul_rn(wt[6], r1)));
+      res[k] = acc.x;
+      res[k + 1] = acc.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const float l = (k == 0) ? dl : c.at(k - 1);
+      const float r = (k == V - 1) ? dr : c.at(k + 1);
+      float acc = __fmul_rn(wt[0], c.at(k));
+      acc = __fadd_rn(acc, __fmul_rn(wt[1], dn.at(k)));
+      acc = __fadd_rn(acc, __fmul_rn(wt[2], up.at(k)));
+      acc = __fadd_rn(acc, __fmul_rn(wt[3], a.at(k)));
+      acc = __fadd_rn(acc, __fmul_rn(wt[4], b.at(k)));
+      acc = __fadd_rn(acc, __fmul_rn(wt[5], l));
+      acc = __fadd_rn(acc, __fmul_rn(wt[6], r));
+      res[k] = acc;
+    }
   }
 }
 

@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(S3Rows<TS>::kThreads, S3Rows<TS>::kMinBlocks)
         const Vt& a = (j == 0) ? wm : cur[j > 0 ? j - 1 : 0];
         const Vt& b = (j == kRW - 1) ? wp : cur[j < kRW - 1 ? j + 1 : 0];
         float res[V], stored[V];
-        cross7_row(p.wt, wt2, nz, cur[j], dn[j], up[j], a, b, dl, dr, res);
+        cross7_row<sizeof(TS) == 2>(p.wt, wt2, nz, cur[j], dn[j], up[j], a, b, dl, dr, res);
         uint32_t o[4];
         if constexpr (sizeof(TS) == 4) {
 #pragma unroll

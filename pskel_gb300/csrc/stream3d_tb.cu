@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           if (lane == 0) dl = el;
           if (lane == 31) dr = er;
           float res[V], stored[V];
-          cross7_row(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
+          cross7_row<true>(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
           const bool valid = plane_in && d_ok && w < W;
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           if (lane == 0) dl = el;
           if (lane == 31) dr = er;
           float res[V], stored[V];
-          cross7_row(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
+          cross7_row<true>(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
           if (!(plane_in && d_ok && w >= 0 && w < W)) o[0] = o[1] = o[2] = o[3] = hraw;
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(kTbThreads, 3)
           if (lane == 0) dl = el;
           if (lane == 31) dr = er;
           float res[V], stored[V];
-          cross7_row(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
+          cross7_row<true>(wt, wt2, nz, c, dn, up, a, b, dl, dr, res);
           uint32_t o[4];
           pack_row<TS>(res, o, stored);
           if (d_ok && w0 + rb + j < W) {

@@ -328,7 +328,8 @@ PSKEL_API pskel_status pskel_set_cost_model(pskel_mlp* m);
  * `polls` polls (1..2^20), then records the timeout in the device error word
  * and returns; which = 2 launches the persistent Life kernel at pass 1 of a
  * run whose pass 0 never ran, with a dependency-wait limit of `polls`, so its
- * own wait runs out and its blocks stop. The next pskel_sync(stream) reports
+ * own wait runs out and its blocks stop; which = 3 does the same with the
+ * persistent multi-pass 2D kernel (a Jacobi run whose first pass is skipped). The next pskel_sync(stream) reports
  * PSKEL_ERR_DEVICE (and clears it); the context stays usable. */
 PSKEL_API pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* stream);
 

@@ -413,6 +413,7 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
   const int mp_per_sm = (S <= 4) ? 2 : 1;
   bool multipass = passes.size() >= 2 && ntiles <= 3 * mp_per_sm * c->sms;
   if (const char* ev = getenv("PSKEL_FAST2D_MULTIPASS")) multipass = passes.size() >= 2 && ev[0] == '1';
+  if (dep_wait_test().spin_limit) multipass = passes.size() >= 2;  // the bounded-wait self-test
   if (multipass) {
     const size_t sync_bytes = fast2d_multipass_sync_bytes(ntiles);
     if (pskel_status q = ensure_buffer(c->fast2d_sync, sync_bytes)) return q;

@@ -30,6 +30,7 @@ struct DeviceContext {
   DeviceBuffer life_sync;                          // Life: item counter and per-tile pass counts
   DeviceBuffer fast2d_sync;                        // 2D multi-pass launches: item counter and per-tile pass counts
   DeviceBuffer tiles;                              // out-of-core runs: slab slots and both arrays' rings
+  DeviceBuffer selftest;                           // the bounded-wait self-test's grids
 };
 
 pskel_status fail(pskel_status code, const char* fmt, ...);

@@ -151,6 +151,16 @@ cudaError_t fast2d_pass(int opk, int dtype, int S, const CUtensorMap* ms, const 
 // per-tile completion counts.
 size_t fast2d_multipass_smem_bytes(int dtype, int S);
 size_t fast2d_multipass_sync_bytes(int ntiles);
+// Self-test of the multi-pass kernel's dependency waits
+// (pskel_selftest_bounded_wait): while set on the calling thread, the next
+// multi-pass 2D run hands out its items from pass `skip_passes` on (the
+// earlier passes never run) and gives a dependency wait up after `spin_limit`
+// polls. Zero (the default): no effect.
+struct DepWaitTest {
+  unsigned spin_limit;
+  int skip_passes;
+};
+DepWaitTest& dep_wait_test();
 cudaError_t fast2d_multipass(int opk, int dtype, int S, const CUtensorMap* map_in, const CUtensorMap* map_out,
                              const Stencil2DParams& p, int npasses, int q, int r, void* sync, int ctas,
                              cudaStream_t s);

@@ -2,14 +2,16 @@
 // kernel waits on an mbarrier phase that never completes, or on a device flag
 // that nothing sets, with a short poll limit; or the persistent Life kernel
 // itself is launched at pass 1 of a run whose pass 0 never ran, so the
-// dependency wait of its first item runs out. The wait gives up, records the
+// dependency wait of its first item runs out (likewise the multi-pass 2D
+// kernel with its first pass skipped). The wait gives up, records the
 // timeout in the device error word and returns (the Life kernel's other blocks
 // see the latched word and stop), so the host reads PSKEL_ERR_DEVICE from
 // pskel_sync and the context stays usable. Nothing faults, traps or hangs.
-#include "../../include/pskel_gb300.h"
-#include "capi_internal.h"
 #include <algorithm>
 #include <cstring>
+
+#include "../../include/pskel_gb300.h"
+#include "capi_internal.h"
 
 #include "common.cuh"
 #include "kernels.h"
@@ -52,8 +54,8 @@ extern "C" {
 
 pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* stream) {
   clear_error();
-  if (which < 0 || which > 2 || polls == 0 || polls > (1u << 20))
-    return fail(PSKEL_ERR_INVALID, "selftest: which must be 0, 1 or 2 and polls in 1..2^20");
+  if (which < 0 || which > 3 || polls == 0 || polls > (1u << 20))
+    return fail(PSKEL_ERR_INVALID, "selftest: which must be 0..3 and polls in 1..2^20");
   DeviceContext* c = nullptr;
   if (pskel_status s = get_context(&c)) return s;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -61,6 +63,33 @@ pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* st
     selftest_wait_kernel<<<1, 32, 0, s>>>(which, polls, c->err);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PSKEL_OK : cuda_fail(e, "selftest launch");
+  }
+  if (which == 3) {
+    // the persistent multi-pass 2D kernel: Jacobi fp32 on a 256 x 256 grid of
+    // zeros, two passes of 11 steps in one launch, items handed out from pass
+    // 1 on: every item waits for pass 0, which never runs
+    const int64_t n = 256;
+    if (pskel_status q = ensure_buffer(c->selftest, 2 * n * n * sizeof(float))) return q;
+    float* A = static_cast<float*>(c->selftest.ptr);
+    const cudaError_t e = cudaMemsetAsync(A, 0, 2 * n * n * sizeof(float), s);
+    if (e != cudaSuccess) return cuda_fail(e, "selftest set-up");
+    static const int32_t offsets[8] = {-1, 0, 1, 0, 0, -1, 0, 1};
+    static const float weights[4] = {0.25f, 0.25f, 0.25f, 0.25f};
+    pskel_stencil st;
+    memset(&st, 0, sizeof(st));
+    st.op = PSKEL_OP_LINEAR;
+    st.dtype = PSKEL_F32;
+    st.mask.size = 4;
+    st.mask.dimension = 2;
+    st.mask.offsets = offsets;
+    st.mask.weights = weights;
+    pskel_schedule sch;
+    memset(&sch, 0, sizeof(sch));
+    sch.time_steps = 11;
+    dep_wait_test() = DepWaitTest{polls, 1};
+    const pskel_status q = pskel_iterate2d(&st, A, A + n * n, n, n, n, 22, &sch, stream);
+    dep_wait_test() = DepWaitTest{0u, 0};
+    return q;
   }
   // the Life kernel on a 512 x 512 grid of zeros, launched for pass 1 only with
   // cleared completion counts: every item waits for pass 0, which never ran

@@ -132,8 +132,10 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
 // One run of fast2d_multipass_kernel: the pass plan and the shared counters.
 struct Fast2DRun {
   int npasses, q, r;              // pass i has 1 + 2 * (q + (i < r)) steps
-  unsigned long long* next_item;  // next (pass, tile) item to hand out
+  unsigned long long* next_item;  // next (pass, tile) item to hand out, counted from first_item
   unsigned* done;                 // passes completed, one count per tile
+  long long first_item;           // 0 (the bounded-wait self-test starts later)
+  unsigned spin_limit;            // polls of one dependency wait before it gives up
 };
 
 constexpr unsigned kFastSpinLimit = 1u << 24;  // polls of a neighbour's completion count (each with a sleep)
@@ -196,7 +198,8 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
   const int dx = (p.HX + p.TW - 1) / p.TW;
   uint32_t phase_bits = 0;  // bit i: parity of the next completion of bars[i]
   for (;;) {
-    if (tid == 0) s_item = error_latched(p.err) ? nitems : static_cast<long long>(atomicAdd(run.next_item, 1ull));
+    if (tid == 0)
+      s_item = error_latched(p.err) ? nitems : run.first_item + static_cast<long long>(atomicAdd(run.next_item, 1ull));
     __syncthreads();
     const long long item = s_item;
     if (item >= nitems) break;
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
                 ok = 0;
                 break;
               }
-              if (++polls >= kFastSpinLimit) {
+              if (++polls >= run.spin_limit) {
                 atomicOr(p.err, kDevErrBarrier);
                 ok = 0;
                 break;
@@ -397,6 +400,11 @@ size_t fast2d_multipass_smem_bytes(int dtype, int S) {
 
 size_t fast2d_multipass_sync_bytes(int ntiles) { return 16 + 4 * static_cast<size_t>(ntiles); }
 
+DepWaitTest& dep_wait_test() {
+  thread_local DepWaitTest t{0u, 0};
+  return t;
+}
+
 cudaError_t fast2d_multipass(int opk, int dtype, int S, const CUtensorMap* map_in, const CUtensorMap* map_out,
                              const Stencil2DParams& p, int npasses, int q, int r, void* sync, int ctas,
                              cudaStream_t s) {
@@ -409,6 +417,9 @@ cudaError_t fast2d_multipass(int opk, int dtype, int S, const CUtensorMap* map_i
   run.r = r;
   run.next_item = static_cast<unsigned long long*>(sync);
   run.done = reinterpret_cast<unsigned*>(static_cast<char*>(sync) + 16);
+  const DepWaitTest& t = dep_wait_test();
+  run.first_item = static_cast<long long>(t.skip_passes) * ntiles;
+  run.spin_limit = t.spin_limit ? t.spin_limit : kFastSpinLimit;
   if (dtype == 2)
     return S == 8 ? dispatch_multipass<__nv_bfloat16, 8>(opk, map_in, map_out, p, run, ctas, s)
                   : dispatch_multipass<__nv_bfloat16, 4>(opk, map_in, map_out, p, run, ctas, s);

@@ -106,7 +106,7 @@ def test_pass_plan_parity():
 def test_selftest_rejects_bad_arguments():
     # argument checks come before any device work
     import pskel_gb300 as P
-    assert P.lib.pskel_selftest_bounded_wait(3, 10, None) == P.PSKEL_ERR_INVALID
+    assert P.lib.pskel_selftest_bounded_wait(4, 10, None) == P.PSKEL_ERR_INVALID
     assert P.lib.pskel_selftest_bounded_wait(-1, 10, None) == P.PSKEL_ERR_INVALID
     assert P.lib.pskel_selftest_bounded_wait(0, 0, None) == P.PSKEL_ERR_INVALID
     assert P.lib.pskel_selftest_bounded_wait(1, (1 << 20) + 1, None) == P.PSKEL_ERR_INVALID

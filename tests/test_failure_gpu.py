@@ -1,7 +1,8 @@
 """Failure detection without a GPU fault: every wait in the library's kernels
 is bounded. A self-test kernel waits on an mbarrier phase that never completes
-and on a device flag that nothing sets, and the persistent Life kernel is
-launched at pass 1 of a run whose pass 0 never ran (its real dependency wait);
+and on a device flag that nothing sets, and the persistent Life and
+multi-pass 2D kernels are started at pass 1 of runs whose pass 0 never ran
+(their real dependency waits);
 each gives up after a few polls and latches the timeout in the device error
 word; the host reads it as PSKEL_ERR_DEVICE and the next call on the same
 context succeeds."""
@@ -18,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("which,word", [(0, "TMA/mbarrier wait timed out"), (1, "dependency wait"),
-                                        (2, "dependency wait")])
+                                        (2, "dependency wait"), (3, "dependency wait")])
 def test_bounded_wait_times_out_and_reports(cuda, oracle_mod, which, word):
     P._check(P.lib.pskel_selftest_bounded_wait(which, 1000, None))
     with pytest.raises(P.PskelError) as ei:

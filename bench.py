@@ -45,9 +45,9 @@ WORKLOADS = {
     "life": dict(desc="Game of Life 2D Moore 8-neighbour mask, uint8 Bernoulli(0.3), 8192x8192, 1000 iterations",
                  W=8192, H=8192, iters=1000, dtype="u8", T=13, b_alg=2),
     "jacobi": dict(desc="Jacobi 2D 5-point (4 neighbours, weight 0.25), float32 1024x1024, zero ring, 100 iterations",
-                   W=1024, H=1024, iters=100, dtype="f32", T=11, b_alg=8),
+                   W=1024, H=1024, iters=100, dtype="f32", T=13, b_alg=8),
     "jacobi_bf16": dict(desc="Jacobi 2D 5-point, bf16 storage / fp32 arithmetic, 1024x1024, 100 iterations",
-                        W=1024, H=1024, iters=100, dtype="bf16", T=11, b_alg=4),
+                        W=1024, H=1024, iters=100, dtype="bf16", T=13, b_alg=4),
     "advect": dict(desc="advection-diffusion 2D, float32 4096x4096, winds N(0,0.1), K 0.1, dt 0.2, 500 iterations",
                    W=4096, H=4096, iters=500, dtype="f32", T=5, b_alg=16),
     "advect_bf16": dict(desc="advection-diffusion 2D, bf16 storage / fp32 arithmetic, 4096x4096, 500 iterations",
@@ -886,12 +886,33 @@ def cpu_baseline(wl, updates):
     return {"value": round(v, 4), "unit": "GCells/s", "cores": os.cpu_count() or 1, "kind": kind, "sample": sample}
 
 
+FP64_ERRORS = Path(__file__).resolve().parent / "tests" / "golden" / "fp64_errors.json"
+
+
+def fp64_error(wl):
+    """The workload's error against an FP64 oracle. The results are
+    bit-identical to the oracle's fp32 / bf16 restatement on these inputs (the
+    -m gpu suite checks the full-size runs), so the error is that of the
+    restatement against the same algorithm in double precision, computed once
+    on the CPU by tests/golden/make_fp64_errors.py."""
+    if wl["name"] == "life":
+        return {"kind": "integer", "note": "bit-exact against the reference; no floating point"}
+    try:
+        e = json.loads(FP64_ERRORS.read_text())[wl["name"]]
+    except (OSError, KeyError, ValueError):
+        return None
+    return {"max_abs": e["max_abs"], "max_rel": e["max_rel"], "rel_l2": e["rel_l2"],
+            "source": "tests/golden/fp64_errors.json (the oracle's bit-identical restatement against FP64 on the "
+                      "same inputs)"}
+
+
 def run_workload(name, args, world, rank, local, cpu_updates):
     import torch
     wl = dict(WORKLOADS[name], name=name)
     runner = run_batch if wl.get("batch") else run_ours
     line, clocks = runner(args, wl, world, rank, local)
     line["clocks"] = clocks
+    line["fp64_error"] = fp64_error(wl)
     finish_roofline(line, name, clocks, torch.cuda.get_device_properties(local).multi_processor_count)
     if rank == 0 and cpu_updates:
         line["cpu_baseline"] = cpu_baseline(wl, cpu_updates)
@@ -901,7 +922,7 @@ def run_workload(name, args, world, rank, local, cpu_updates):
 def compact(line):
     """The keys of another workload's line that the headline line carries."""
     out = {k: line[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "dtype", "config", "schedule",
-                                "gpu_launches", "roofline", "cpu_baseline", "clocks") if k in line}
+                                "gpu_launches", "roofline", "cpu_baseline", "clocks", "fp64_error") if k in line}
     out["plain"] = line["plain"].get("value") if isinstance(line.get("plain"), dict) else None
     out["e2e"] = line["e2e"]["value"]
     if "tuning" in line:

@@ -124,13 +124,14 @@ cudaError_t stencil2d_pass(Op2D op, int dtype, bool use_tma, const CUtensorMap* 
 int fast2d_shape(const int* offsets, int n);
 // The default steps per pass of the reach-1 kernels (measured on GB300):
 // linear shapes 7 (4096^2 fp32: T=5/7 1.32/1.30 T cell updates/s, T=1 0.70),
-// 11 on grids of at most 1M cells, which run every pass in one launch and
-// have fewer tiles than resident CTAs (1024^2 fp32: T=7/11/13 515/594/602
-// G cell updates/s; 1448^2: T=7/11 928/897);
+// 13 on grids of at most 1M cells, which run every pass in one launch and
+// have fewer tiles than resident CTAs (1024^2 fp32: T=7/9/11/13/15/17
+// 582/638/681/712/700/690 G cell updates/s: 286 tiles at T=13 put two on
+// nearly every SM; 1448^2: T=7/11 928/897);
 // advection fp32 5; advection bf16 1 (the HBM-bound streaming kernel) on
 // grids of 4M cells or more, else 7.
 inline int fast2d_default_steps(bool advect, int dtype, int64_t W, int64_t H) {
-  if (!advect) return W * H <= (int64_t(1) << 20) ? 11 : 7;
+  if (!advect) return W * H <= (int64_t(1) << 20) ? 13 : 7;
   if (dtype != 2) return 5;
   return W * H >= (int64_t(1) << 22) ? 1 : 7;
 }

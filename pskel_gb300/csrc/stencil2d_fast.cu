@@ -213,28 +213,33 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     const bool ring_tile = (gy0 < p.ring) || (gy0 + LH > p.H - p.ring) || (gx0 < p.ring) || (gx0 + LW > p.W - p.ring);
     const bool stage_dst = ring_tile && steps >= 2;
     int ok = 1;
-    if (tid == 0) {
+    if (tid < 32) {
       if (pass > 0) {
-        for (int yy = max(0, ty - dy); yy <= min(p.tiles_y - 1, ty + dy) && ok; ++yy) {
-          for (int xx = max(0, tx - dx); xx <= min(p.tiles_x - 1, tx + dx) && ok; ++xx) {
-            const unsigned* d = &run.done[yy * p.tiles_x + xx];
-            unsigned polls = 0;
-            while (ld_acquire_gpu(d) < static_cast<unsigned>(pass)) {
-              if (error_latched(p.err)) {  // another CTA gave up and reported why
-                ok = 0;
-                break;
-              }
-              if (++polls >= run.spin_limit) {
-                atomicOr(p.err, kDevErrBarrier);
-                ok = 0;
-                break;
-              }
-              __nanosleep(32);
+        // the lanes of warp 0 wait for one neighbour tile each, so the
+        // acquire loads' round trips overlap instead of adding up
+        const int y0 = max(0, ty - dy), x0 = max(0, tx - dx);
+        const int nx = min(p.tiles_x - 1, tx + dx) - x0 + 1;
+        const int nn = (min(p.tiles_y - 1, ty + dy) - y0 + 1) * nx;
+        for (int i = tid; i < nn && ok; i += 32) {
+          const unsigned* d = &run.done[(y0 + i / nx) * p.tiles_x + x0 + i % nx];
+          unsigned polls = 0;
+          while (ld_acquire_gpu(d) < static_cast<unsigned>(pass)) {
+            if (error_latched(p.err)) {  // another CTA gave up and reported why
+              ok = 0;
+              break;
             }
+            if (++polls >= run.spin_limit) {
+              atomicOr(p.err, kDevErrBarrier);
+              ok = 0;
+              break;
+            }
+            __nanosleep(32);
           }
         }
+        ok = __all_sync(0xFFFFFFFFu, ok);
+        __syncwarp();  // orders every lane's acquire before lane 0's load below
       }
-      if (ok) {
+      if (ok && tid == 0) {
         // the previous pass wrote through the generic proxy, TMA reads through
         // the async proxy; the buffers were last read by this CTA's threads
         fence_proxy_async_global();
@@ -270,9 +275,11 @@ __global__ void __launch_bounds__(kFastThreads, S <= 4 ? 2 : 1)
     g.v = p.v;
     TS* dst = static_cast<TS*>(fwd ? p.dst : const_cast<void*>(p.src));
     fast2d_run_tile<TS, OpK, S>(buf0, buf1, dst, g, gy0, gx0, ring_tile, wt, neg_zero2(p.fuse_guard));
-    __threadfence();
+    // the block's write-back is ordered before thread 0's release by the
+    // barrier; one gpu-scope fence then publishes all of it
     __syncthreads();
     if (tid == 0) {
+      __threadfence();
       fence_proxy_async_global();
       atomicAdd(&run.done[tile], 1u);
     }

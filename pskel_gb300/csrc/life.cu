@@ -336,14 +336,11 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
 
   if (w == NW) {
     // ---------------------------------------------------------- producer
-    // lane 0 takes the items and issues the loads; the lanes wait for one
-    // tile of the previous pass each, so the acquire loads overlap
+    if (lane != 0) return;
     const int dy = (T + TH - 1) / TH;
     uint32_t empty_phase = 0;
     for (long long k = 0;; ++k) {
-      long long it = 0;
-      if (lane == 0) it = error_latched(err) ? nitems : static_cast<long long>(atomicAdd(next_item, 1ull));
-      it = __shfl_sync(0xFFFFFFFFu, it, 0);
+      const long long it = error_latched(err) ? nitems : static_cast<long long>(atomicAdd(next_item, 1ull));
       int valid = it < nitems ? 1 : 0;
       int pass = 0, tile = 0;
       if (valid) {
@@ -361,56 +358,49 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
       const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
       if (valid && pass > 0) {
         const unsigned need = static_cast<unsigned>(pass) * NW;
-        const int y0 = max(0, ty - dy), x0 = max(0, tx - 1);
-        const int nx = min(tiles_x - 1, tx + 1) - x0 + 1;
-        const int nn = (min(tiles_y - 1, ty + dy) - y0 + 1) * nx;
-        int ok = 1;
-        for (int i = lane; i < nn && ok; i += 32) {
-          const unsigned* d = &done[(y0 + i / nx) * tiles_x + x0 + i % nx];
-          unsigned polls = 0;
-          while (ld_acquire_u32(d) < need) {
-            if (error_latched(err)) {  // another block gave up: stop, it reported why
-              ok = 0;
-              break;
+        for (int yy = max(0, ty - dy); yy <= min(tiles_y - 1, ty + dy) && valid; ++yy) {
+          for (int xx = max(0, tx - 1); xx <= min(tiles_x - 1, tx + 1) && valid; ++xx) {
+            const unsigned* d = &done[yy * tiles_x + xx];
+            unsigned polls = 0;
+            while (ld_acquire_u32(d) < need) {
+              if (error_latched(err)) {  // another block gave up: stop, it reported why
+                valid = 0;
+                break;
+              }
+              if (++polls >= spin_limit) {
+                atomicOr(err, kDevErrBarrier);
+                valid = 0;
+                break;
+              }
+              __nanosleep(32);
             }
-            if (++polls >= spin_limit) {
-              atomicOr(err, kDevErrBarrier);
-              ok = 0;
-              break;
-            }
-            __nanosleep(32);
           }
         }
-        valid = __all_sync(0xFFFFFFFFu, ok);
-        __syncwarp();  // orders every lane's acquire before lane 0's load below
       }
-      if (lane == 0) {
-        // the consumers have copied the previous window (and read its slot)
-        if (k > 0) {
-          if (!mbar_wait_bounded(empty, empty_phase, err)) valid = 0;
-          empty_phase ^= 1u;
-        }
-        slot->valid = valid;
-        slot->pass = pass;
-        slot->tile = tile;
-        if (!valid) {
-          mbar_arrive(full);  // releases the consumers with valid = 0
-        } else {
-          const int wy0 = ty * TH - T;
-          const int gx = tx * kLifeCoreWords - 1;
-          const bool ring_tile = wy0 < ring || wy0 + G::kWindowRows > H - ring || gx * 32 < ring ||
-                                 (gx + 32) * 32 > W - ring;
-          const CUtensorMap* msrc = (pass & 1) ? &mapY : &mapX;
-          const CUtensorMap* mdst = (pass & 1) ? &mapX : &mapY;
-          // the tiles awaited above wrote through the generic proxy; TMA
-          // reads through the async proxy
-          fence_proxy_async_global();
-          mbar_arrive_expect_tx(full, G::kBoxBytes * (ring_tile ? 2u : 1u));
-          tma_load_2d(win_src, msrc, gx & ~3, wy0, full);
-          if (ring_tile) tma_load_2d(win_dst, mdst, gx & ~3, wy0, full);
-        }
+      // the consumers have copied the previous window (and read its slot)
+      if (k > 0) {
+        if (!mbar_wait_bounded(empty, empty_phase, err)) valid = 0;
+        empty_phase ^= 1u;
       }
-      if (!__shfl_sync(0xFFFFFFFFu, valid, 0)) return;  // the whole warp leaves together
+      slot->valid = valid;
+      slot->pass = pass;
+      slot->tile = tile;
+      if (!valid) {
+        mbar_arrive(full);  // releases the consumers with valid = 0
+        return;
+      }
+      const int wy0 = ty * TH - T;
+      const int gx = tx * kLifeCoreWords - 1;
+      const bool ring_tile = wy0 < ring || wy0 + G::kWindowRows > H - ring || gx * 32 < ring ||
+                             (gx + 32) * 32 > W - ring;
+      const CUtensorMap* msrc = (pass & 1) ? &mapY : &mapX;
+      const CUtensorMap* mdst = (pass & 1) ? &mapX : &mapY;
+      // the tiles awaited above wrote through the generic proxy; TMA reads
+      // through the async proxy
+      fence_proxy_async_global();
+      mbar_arrive_expect_tx(full, G::kBoxBytes * (ring_tile ? 2u : 1u));
+      tma_load_2d(win_src, msrc, gx & ~3, wy0, full);
+      if (ring_tile) tma_load_2d(win_dst, mdst, gx & ~3, wy0, full);
     }
   }
 

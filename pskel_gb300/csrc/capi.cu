@@ -337,12 +337,24 @@ static pskel_status iterate_fast2d(const pskel_stencil& st, int opk, void* in, v
   if (T == 1) {
     // one step per pass: the streaming kernel with rows staged by TMA,
     // persistent blocks over items of 32 vectors of columns x HC rows
-    // (tile_h; default: about four items per resident block, 8-row groups)
+    // (tile_h; by default a multiple of 8 rows, at least 32, chosen like the
+    // 3D h chunks: block b takes items b, b + ctas, ..., so the busiest block
+    // streams ceil(items / ctas) items of about HC + 8 rows (its 8-row boxes);
+    // the HC minimising that, then the rows loaded in all, wins)
     const int esz = dtype == PSKEL_BF16 ? 2 : 4;
     const int64_t resident = static_cast<int64_t>(stream2d_tma_blocks_per_sm(opk, dtype)) * c->sms;
     const int64_t strips = stream2d_tma_items(static_cast<int>(W), static_cast<int>(H), static_cast<int>(H), dtype);
-    int HC = static_cast<int>((H * strips + 4 * resident - 1) / (4 * resident));
-    HC = std::max(32, ((HC + 7) / 8) * 8);
+    int HC = 32;
+    double best = 0.0;
+    for (int64_t hc = 32; hc < H + 8; hc += 8) {
+      const int64_t items = strips * ((H + hc - 1) / hc), used = std::min<int64_t>(items, resident);
+      const double cost = static_cast<double>((items + used - 1) / used) * static_cast<double>(hc + 8) +
+                          1e-3 * static_cast<double>(items * (hc + 8)) / static_cast<double>(resident);
+      if (hc == 32 || cost < best) {
+        best = cost;
+        HC = static_cast<int>(hc);
+      }
+    }
     if (sched && sched->tile_h > 0) HC = static_cast<int>(std::min<int64_t>(sched->tile_h, H));
     p.TH = HC;
     p.tiles_y = static_cast<int>((H + HC - 1) / HC);

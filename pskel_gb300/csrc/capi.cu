@@ -659,6 +659,38 @@ static std::vector<int> plan_tb2(int64_t iters) {
   return p;
 }
 
+// h chunks of a streaming 3D launch (items of at least `min_planes` planes,
+// or tile_h planes): block b takes items b, b + ctas, ..., so a launch lasts
+// as long as its busiest block, which streams ceil(items / ctas) items of
+// HC + `halo` planes each (the planes an item loads). The count minimising
+// that, then the planes loaded in all (halo re-reads), wins. Measured on
+// 512^3 heat against about four (one step) or two (two steps) items per
+// block: bf16 one step 29 -> 7 chunks 1277 -> 1301 GCells/s, bf16 two steps
+// 15 -> 7 chunks 1157 -> 1207, fp32 two steps 8 -> 7 chunks 1038 -> 1052
+// (fp32 one step keeps 19).
+static void configure_hchunks(Stencil3DParams& q, int64_t W, int64_t H, int64_t D, int esz, int64_t resident,
+                              int halo, int64_t min_planes, const pskel_schedule* sched, int64_t& ctas) {
+  const int64_t cols = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), 1, esz);
+  int64_t chunks = 1;
+  double best = 0.0;
+  for (int64_t k = 1; k <= std::max<int64_t>(1, H / min_planes); ++k) {
+    const int64_t hc = (H + k - 1) / k, hk = (H + hc - 1) / hc;
+    const int64_t items = cols * hk, used = std::min<int64_t>(items, resident);
+    const double cost = static_cast<double>((items + used - 1) / used) * static_cast<double>(hc + halo) +
+                        1e-3 * static_cast<double>(items * (hc + halo)) / static_cast<double>(resident);
+    if (k == 1 || cost < best) {
+      best = cost;
+      chunks = k;
+    }
+  }
+  if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
+  q.HC = static_cast<int>((H + chunks - 1) / chunks);
+  q.hchunks = static_cast<int>((H + q.HC - 1) / q.HC);
+  const int64_t items = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), q.hchunks, esz);
+  ctas = std::min<int64_t>(items, resident);
+  if (sched && sched->ctas > 0) ctas = std::min<int64_t>(ctas, sched->ctas);
+}
+
 // The 7-point cross, one step per launch, planes staged by TMA: persistent
 // blocks over work items of (32 vectors of d) x 16 w x HC planes, about four
 // items per resident block.
@@ -671,36 +703,8 @@ static pskel_status stream3d_cross7(const pskel_stencil& st, Stencil3DParams& p,
   const std::vector<int> passes = steps == 2 ? plan_tb2(iters) : std::vector<int>(static_cast<size_t>(iters), 1);
   const bool any2 = !passes.empty() && passes.front() == 2;
   const bool any1 = !passes.empty() && passes.back() == 1;
-  const int64_t cols = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), 1, esz);
-  // h chunks (items of at least `min_planes` planes, or tile_h planes): block
-  // b takes items b, b + ctas, ..., so a launch lasts as long as its busiest
-  // block, which streams ceil(items / ctas) items of HC + `halo` planes each
-  // (the planes an item loads). The count minimising that, then the planes
-  // loaded in all (halo re-reads), wins. Measured on 512^3 heat against
-  // about four (one step) or two (two steps) items per block: bf16 one step
-  // 29 -> 7 chunks 1277 -> 1301 GCells/s, bf16 two steps 15 -> 7 chunks
-  // 1157 -> 1207, fp32 two steps 8 -> 7 chunks 1038 -> 1052 (fp32 one step
-  // keeps 19).
   auto configure = [&](Stencil3DParams& q, int per_sm, int halo, int64_t min_planes, int64_t& ctas) {
-    const int64_t resident = static_cast<int64_t>(per_sm) * c->sms;
-    int64_t chunks = 1;
-    double best = 0.0;
-    for (int64_t k = 1; k <= std::max<int64_t>(1, H / min_planes); ++k) {
-      const int64_t hc = (H + k - 1) / k, hk = (H + hc - 1) / hc;
-      const int64_t items = cols * hk, used = std::min<int64_t>(items, resident);
-      const double cost = static_cast<double>((items + used - 1) / used) * static_cast<double>(hc + halo) +
-                          1e-3 * static_cast<double>(items * (hc + halo)) / static_cast<double>(resident);
-      if (k == 1 || cost < best) {
-        best = cost;
-        chunks = k;
-      }
-    }
-    if (sched && sched->tile_h > 0) chunks = std::max<int64_t>(1, (H + sched->tile_h - 1) / sched->tile_h);
-    q.HC = static_cast<int>((H + chunks - 1) / chunks);
-    q.hchunks = static_cast<int>((H + q.HC - 1) / q.HC);
-    const int64_t items = stream3d_tma_items(static_cast<int>(W), static_cast<int>(D), q.hchunks, esz);
-    ctas = std::min<int64_t>(items, resident);
-    if (sched && sched->ctas > 0) ctas = std::min<int64_t>(ctas, sched->ctas);
+    configure_hchunks(q, W, H, D, esz, static_cast<int64_t>(per_sm) * c->sms, halo, min_planes, sched, ctas);
   };
   Stencil3DParams p2 = p;
   int64_t ctas1 = 0, ctas2 = 0;
@@ -1276,7 +1280,9 @@ pskel_status pskel_iterate3d(const pskel_stencil* st, void* in, void* out, int64
 // band still reads. The middle steps run over the whole grid; the last Tw
 // steps run as a second wavefront from the complete state, and the planes
 // each of its rounds leaves final go back to the host on a third stream while
-// the next rounds compute. Residual steps add each band's squared-difference
+// the next rounds compute. With two steps per pass (the fp32 default), the
+// middle steps run as pairs of two-step passes (a pair leaves the state in
+// the buffer the step-by-step run has it in). Residual steps add each band's squared-difference
 // sum to the step's accumulator in launch order (deterministic), square roots
 // at the end. Results equal pskel_iterate3d's bit for bit (the norms up to
 // the grouping of the fp64 sums).
@@ -1287,14 +1293,14 @@ static bool wavefront3d_applies(const pskel_stencil& st, int64_t H, int64_t D, i
   uint32_t hb;
   std::memcpy(&hb, &st.mask.halo_value, sizeof(hb));
   const bool halo_exact = st.dtype != PSKEL_BF16 || (hb & 0xFFFFu) == 0u;
-  const bool plain = !sched || (sched->time_steps <= 1 && sched->tile_h == 0 && sched->ctas == 0);
+  const bool plain = !sched || (sched->time_steps <= 2 && sched->tile_h == 0 && sched->ctas == 0);
   return plain && halo_exact && iters >= 2 && iters <= 256 && H >= 128 && (every == 0 || iters / every <= 4096) &&
          stream3d_is_cross7(st.mask.offsets, st.mask.size, D, static_cast<int>(esz));
 }
 
 static pskel_status run3d_wavefront(const pskel_stencil& st, int64_t W, int64_t H, int64_t D, int64_t iters,
                                     int64_t every, const void* in_host, void* out_host, double* residuals_host,
-                                    DeviceContext* c) {
+                                    const pskel_schedule* sched, DeviceContext* c) {
   const int dtype = static_cast<int>(st.dtype);
   const int esz = static_cast<int>(dtype_size(st.dtype));
   const size_t plane = static_cast<size_t>(W) * D * esz;
@@ -1322,19 +1328,31 @@ static pskel_status run3d_wavefront(const pskel_stencil& st, int64_t W, int64_t 
   p.halo = st.mask.halo_value;
   p.err = c->err;
   double* acc = nullptr;
+  // the middle steps two per pass when that is the schedule (fp32's default)
+  const int ts = sched ? sched->time_steps : 0;
+  const bool two = ts == 2 || (ts == 0 && cross7_default_steps(st.dtype) == 2);
+  Stencil3DParams p2 = p;
+  int64_t ctas2 = 0;
+  if (two)
+    configure_hchunks(p2, W, H, D, esz, static_cast<int64_t>(stream3d_tb2_blocks_per_sm(dtype)) * c->sms, 4, 16,
+                      nullptr, ctas2);
   if (nres > 0) {
     if (pskel_status q = ensure_buffer(c->residuals, static_cast<size_t>(nres) * sizeof(double))) return q;
     if (pskel_status q = ensure_buffer(c->res_acc, static_cast<size_t>(nres) * sizeof(double))) return q;
-    if (pskel_status q = ensure_buffer(c->partials, static_cast<size_t>(resident) * sizeof(double))) return q;
+    const int64_t need = std::max<int64_t>(resident, 2 * ctas2);
+    if (pskel_status q = ensure_buffer(c->partials, static_cast<size_t>(need) * sizeof(double))) return q;
     acc = static_cast<double*>(c->res_acc.ptr);
-    p.partials = static_cast<double*>(c->partials.ptr);
+    p.partials = p2.partials = static_cast<double*>(c->partials.ptr);
   }
-  CUtensorMap maps[2];
+  CUtensorMap maps[2], maps2[2];
   const uint64_t dims[3] = {static_cast<uint64_t>(D) * esz / 4, static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
   const uint64_t strides[2] = {static_cast<uint64_t>(D) * esz, static_cast<uint64_t>(D) * esz * W};
   const uint32_t box[3] = {136, 18, 1};
+  const uint32_t box2[3] = {136, stream3d_tb2_box_rows(), 1};
   cudaError_t e = encode_tmap(&maps[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, A, dims, strides, box);
   if (e == cudaSuccess) e = encode_tmap(&maps[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, B, dims, strides, box);
+  if (two && e == cudaSuccess) e = encode_tmap(&maps2[0], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, A, dims, strides, box2);
+  if (two && e == cudaSuccess) e = encode_tmap(&maps2[1], CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, B, dims, strides, box2);
   if (e != cudaSuccess) return cuda_fail(e, "cuTensorMapEncodeTiled (3D planes)");
   const int64_t C0 = std::min<int64_t>(16, H / 64);
   const int64_t S = (H + C0 - 1) / C0;
@@ -1394,7 +1412,24 @@ static pskel_status run3d_wavefront(const pskel_stencil& st, int64_t W, int64_t 
       if (lo < up && (e = step(t, lo, up)) != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
     }
   }
-  for (int64_t t = Tw + 1; t <= t_last; ++t)
+  int64_t tm = Tw;  // steps done by the middle phase so far
+  // two-step passes in pairs: the first leaves step tm+2 in the other buffer,
+  // the second brings step tm+4 back to the buffer of step tm
+  auto rep = [&](int64_t t) -> double* { return (nres > 0 && t % every == 0) ? acc + (t / every - 1) : nullptr; };
+  for (; two && tm + 4 <= t_last; tm += 4) {
+    uint8_t* X = (tm % 2 == 0) ? A : B;
+    uint8_t* Y = (X == A) ? B : A;
+    for (int h = 0; h < 2; ++h) {
+      p2.src = h == 0 ? X : Y;
+      p2.dst = h == 0 ? Y : X;
+      p2.steps = 2;
+      p2.step0 = tm + 2 * h;
+      if ((e = stream3d_tb2_band(dtype, &maps2[p2.src == A ? 0 : 1], p2, static_cast<int>(ctas2), rep(tm + 2 * h + 1),
+                                 rep(tm + 2 * h + 2), s)) != cudaSuccess)
+        return cuda_fail(e, "3D stencil kernel launch");
+    }
+  }
+  for (int64_t t = tm + 1; t <= t_last; ++t)
     if ((e = step(t, 0, H)) != cudaSuccess) return cuda_fail(e, "3D stencil kernel launch");
   for (int64_t k = 0; k < C; ++k) {
     for (int64_t t = t_last + 1; t <= iters; ++t) {
@@ -1437,7 +1472,7 @@ pskel_status pskel_run3d_host(const pskel_stencil* st, const void* in_host, void
   if (pskel_status s = get_context(&c)) return s;
   if (wavefront3d_applies(*st, height, depth, iterations, residual_every, sched))
     return run3d_wavefront(*st, width, height, depth, iterations, residual_every, in_host, out_host, residuals_host,
-                           c);
+                           sched, c);
   const size_t bytes = static_cast<size_t>(width) * height * depth * dtype_size(st->dtype);
   if (pskel_status s = ensure_buffer(c->host_in, bytes)) return s;
   if (pskel_status s = ensure_buffer(c->host_out, bytes)) return s;

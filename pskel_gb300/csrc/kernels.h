@@ -253,6 +253,13 @@ cudaError_t stream3d_tma_band(int dtype, const CUtensorMap* map, const Stencil3D
                               cudaStream_t s);
 // residuals[i] = sqrt(acc[i]) for i < n.
 cudaError_t stream3d_finish_residuals(const double* acc, int n, double* residuals, cudaStream_t s);
+// acc[0] += the sum of partials[0..n) (one block, fixed order).
+cudaError_t stream3d_accumulate(const double* partials, int n, double* acc, cudaStream_t s);
+// One two-step pass over the whole grid whose squared-difference sums of its
+// first / second step are added to acc1 / acc2 (each reported when non-null;
+// partials: 2 * ctas doubles).
+cudaError_t stream3d_tb2_band(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas, double* acc1,
+                              double* acc2, cudaStream_t s);
 cudaError_t stencil3d_pass(int dtype, bool use_tma, const CUtensorMap* map_src, const Stencil3DParams& p, int ctas,
                            cudaStream_t s);
 

@@ -742,6 +742,11 @@ cudaError_t stream3d_tma_band(int dtype, const CUtensorMap* map, const Stencil3D
   return cudaGetLastError();
 }
 
+cudaError_t stream3d_accumulate(const double* partials, int n, double* acc, cudaStream_t s) {
+  reduce3d_accumulate<<<1, 256, 0, s>>>(partials, n, acc);
+  return cudaGetLastError();
+}
+
 cudaError_t stream3d_finish_residuals(const double* acc, int n, double* residuals, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   finish3d_residuals<<<(n + 255) / 256, 256, 0, s>>>(acc, n, residuals);

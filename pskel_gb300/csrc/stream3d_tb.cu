@@ -482,4 +482,23 @@ cudaError_t stream3d_tb2_pass(int dtype, const CUtensorMap* map, const Stencil3D
   return stream3d_reduce_residuals(p.partials, ctas, 2, p.step0, p.every, p.residuals, s);
 }
 
+cudaError_t stream3d_tb2_band(int dtype, const CUtensorMap* map, const Stencil3DParams& p, int ctas, double* acc1,
+                              double* acc2, cudaStream_t s) {
+  const int rep = (acc1 ? 1 : 0) | (acc2 ? 2 : 0);
+  uint32_t hbits;
+  std::memcpy(&hbits, &p.halo, sizeof(hbits));
+  const bool zero = hbits == 0u;  // +0.0 exactly: the TMA zero fill is the halo
+  if (dtype == 2) {
+    if (zero) launch_tb2<__nv_bfloat16, true>(map, p, ctas, rep, s);
+    else launch_tb2<__nv_bfloat16, false>(map, p, ctas, rep, s);
+  } else {
+    if (zero) launch_tb2<float, true>(map, p, ctas, rep, s);
+    else launch_tb2<float, false>(map, p, ctas, rep, s);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && acc1) e = stream3d_accumulate(p.partials, ctas, acc1, s);
+  if (e == cudaSuccess && acc2) e = stream3d_accumulate(p.partials + ctas, ctas, acc2, s);
+  return e;
+}
+
 }  // namespace pskel

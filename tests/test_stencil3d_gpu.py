@@ -207,6 +207,24 @@ def test_host_run_wavefront(cuda, oracle_mod, dtype, W, H, D, iters, every, halo
         np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
 
 
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+@pytest.mark.parametrize("iters,every", [(41, 5), (38, 0), (33, 1)])
+@pytest.mark.parametrize("halo", [0.0, 0.5])
+def test_host_run_wavefront_two_step_middle(cuda, oracle_mod, dtype, iters, every, halo):
+    """Two steps per pass (fp32's default, or asked for): the host call's
+    middle steps run as pairs of two-step passes between the band wavefronts,
+    with residual steps inside the pairs; weights whose products round."""
+    keep = P._Keep()
+    a, b = grids(40, 150, 64, iters + 7, dtype)
+    st = P.make_stencil(P.OP_LINEAR, dtype, S.HEAT7_OFFSETS, INEXACT7, halo=halo, keep=keep)
+    got, res = P.run3d_host(st, np.ascontiguousarray(a), np.ascontiguousarray(b).copy(), iters,
+                            sched=dict(time_steps=2, tile_w=0, tile_h=0, tile_d=0, ctas=0), residual_every=every)
+    want, wres = oracle_mod.lin3d(a, b, S.HEAT7_OFFSETS, INEXACT7, iters, halo=halo, dtype=dtype, every=every)
+    assert np.array_equal(bits(got), bits(want))
+    if every:
+        np.testing.assert_allclose(res, wres, rtol=res_rtol(a.shape), atol=0)
+
+
 def test_host_run_wavefront_max_iterations(cuda, oracle_mod):
     keep = P._Keep()
     a, b = grids(32, 160, 32, 5, "f32")

@@ -43,7 +43,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GCells/s"
 WORKLOADS = {
     "life": dict(desc="Game of Life 2D Moore 8-neighbour mask, uint8 Bernoulli(0.3), 8192x8192, 1000 iterations",
-                 W=8192, H=8192, iters=1000, dtype="u8", T=13, b_alg=2),
+                 W=8192, H=8192, iters=1000, dtype="u8", T=17, b_alg=2),
     "jacobi": dict(desc="Jacobi 2D 5-point (4 neighbours, weight 0.25), float32 1024x1024, zero ring, 100 iterations",
                    W=1024, H=1024, iters=100, dtype="f32", T=13, b_alg=8),
     "jacobi_bf16": dict(desc="Jacobi 2D 5-point, bf16 storage / fp32 arithmetic, 1024x1024, 100 iterations",

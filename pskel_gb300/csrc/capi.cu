@@ -221,8 +221,10 @@ static bool tma_ok(const void* p, int64_t pitch_bytes) {
 // planes (L2-resident for grids up to ~16k x 16k), the passes run between the
 // planes, and the final plane's interior is unpacked into the result buffer.
 // The other buffer is not written; ring cells of the result keep their bytes.
-// Generations per pass of the Life kernel by default (measured on GB300, 8192^2).
-constexpr int kLifeDefaultSteps = 13;
+// Generations per pass of the Life kernel by default (measured on GB300,
+// 8192^2, 24 rows per lane: T = 13/15/17/19/21/25 26.9/27.3/27.7/27.2/27.4/27.0
+// T updates/s; at T = 17 its 328-row cores tile the 8192 rows 25 times).
+constexpr int kLifeDefaultSteps = 17;
 
 static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, int64_t W, int64_t H, int64_t pitch,
                                  int64_t iters, int ring, const pskel_schedule* sched, DeviceContext* c,

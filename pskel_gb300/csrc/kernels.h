@@ -30,7 +30,7 @@ std::vector<int> plan_passes(int64_t iters, int T);
 // steps its core of TH <= life_bits_max_tile_h(T) = kLifeWindowRows - 2T rows
 // is exact.
 constexpr int kLifeBitsMaxT = 31;
-constexpr int kLifeRows = 16;
+constexpr int kLifeRows = 24;
 constexpr int kLifeWarps = 15;
 constexpr int kLifeCoreWords = 30;
 constexpr int kLifeWindowRows = kLifeWarps * kLifeRows + 2;

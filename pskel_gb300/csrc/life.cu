@@ -237,9 +237,14 @@ constexpr int kLifeBoxWords = 36;
 template <int R, int NW>
 struct LifeGeo {
   static constexpr int kWindowRows = NW * R + 2;
+  // the window arrives as kBoxes TMA boxes of kBoxRows rows (a box has at
+  // most 256 rows; several boxes have a multiple of 8 rows, so that each
+  // lands 128-byte aligned, and may fetch a few rows past the window)
+  static constexpr int kBoxes = (kWindowRows + 255) / 256;
+  static constexpr int kBoxRows = kBoxes == 1 ? kWindowRows : ((kWindowRows + kBoxes - 1) / kBoxes + 7) / 8 * 8;
   static constexpr int kThreads = (NW + 1) * 32;
   static constexpr int kConsumerThreads = NW * 32;
-  static constexpr uint32_t kBoxBytes = kWindowRows * kLifeBoxWords * 4;
+  static constexpr uint32_t kBoxBytes = kBoxes * kBoxRows * kLifeBoxWords * 4;  // one window's boxes
   static constexpr int kBoxStride = (kBoxBytes + 127) / 128 * 128;
   // shared memory (bytes): source window, destination window (ring tiles),
   // the exchange rows (two parities x warps x {first, last} row x 32 lanes),
@@ -250,7 +255,8 @@ struct LifeGeo {
   static constexpr int kSmemWords = 2 * kBoxStride / 4 + kXchWords + 2 * kRingWords;
   static constexpr size_t kSmemBytes = static_cast<size_t>(kSmemWords) * 4 + 64;
   static_assert(kBoxBytes % 16 == 0, "TMA transaction bytes");
-  static_assert(kWindowRows <= 256, "TMA box rows");
+  static_assert(kBoxRows * kBoxes >= kWindowRows && kBoxRows <= 256, "TMA box rows");
+  static_assert((kBoxRows * kLifeBoxWords * 4) % 128 == 0 || kBoxes == 1, "box destinations 128-byte aligned");
   static_assert(NW <= 15, "one named barrier per neighbouring pair, ids 1..14, and 15 for all consumers");
 };
 
@@ -399,8 +405,12 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
       // through the async proxy
       fence_proxy_async_global();
       mbar_arrive_expect_tx(full, G::kBoxBytes * (ring_tile ? 2u : 1u));
-      tma_load_2d(win_src, msrc, gx & ~3, wy0, full);
-      if (ring_tile) tma_load_2d(win_dst, mdst, gx & ~3, wy0, full);
+#pragma unroll
+      for (int b = 0; b < G::kBoxes; ++b) {
+        const int off = b * G::kBoxRows * kLifeBoxWords;
+        tma_load_2d(win_src + off, msrc, gx & ~3, wy0 + b * G::kBoxRows, full);
+        if (ring_tile) tma_load_2d(win_dst + off, mdst, gx & ~3, wy0 + b * G::kBoxRows, full);
+      }
     }
   }
 
@@ -489,8 +499,10 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
 namespace {
 
 // The kernel as launched: kLifeRows rows per lane, kLifeWarps consumer warps,
-// one block per SM. Measured on GB300 (8192^2, 1000 generations): 16 rows x
-// 15 warps at one block per SM 27.3 T updates/s (T = 15); 8 rows x 15 warps
+// one block per SM. Measured on GB300 (8192^2, 1000 generations): 24 rows x
+// 15 warps (128 registers: the register file exactly; a 362-row window in two
+// TMA boxes) 27.7 T updates/s at T = 17; 16 rows x 15 warps (242 rows, one
+// box) 27.4 T at T = 13, 27.3 T at T = 15; 8 rows x 15 warps
 // at two blocks per SM 21.5 T (T = 7, the best T for it; its windows are half
 // as tall, so the halo rows and the per-step exchange cost twice as much per
 // row); 16 rows x 7 warps at two blocks per SM 22.5 T. The row shifts as
@@ -590,7 +602,7 @@ cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int rin
   CUtensorMap mx, my;
   const uint64_t dims[2] = {static_cast<uint64_t>(PW), static_cast<uint64_t>(H)};
   const uint64_t strides[1] = {static_cast<uint64_t>(PW) * 4};
-  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(LifeKernelGeo::kWindowRows)};
+  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(LifeKernelGeo::kBoxRows)};
   cudaError_t e = encode_tmap(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, X, dims, strides, box);
   if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
   if (e != cudaSuccess) return e;

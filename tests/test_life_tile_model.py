@@ -27,7 +27,7 @@ from pskel_gb300 import synth as S
 CORE = 30  # core words per tile (kernels.h)
 # (consumer warps per block, rows per lane): the kernel's geometry (kernels.h)
 # first; a window half as tall checks the same scheme with more tiles
-VARIANTS = [(15, 16), (15, 8)]
+VARIANTS = [(15, 24), (15, 8)]
 
 
 def words(W):
@@ -195,7 +195,8 @@ def test_tile_model_shorter_tiles(oracle_mod):
 
 
 def test_planted_mistakes_are_caught(oracle_mod):
-    a, b = grids(1000, 300, seed=7)
+    # taller than one core, so that a core boundary falls inside the grid
+    a, b = grids(1000, 700, seed=7)
     want = oracle_mod.life(a, b, 13)
     assert not np.array_equal(model_life(a, b, 13, 13, exchange=False), want)
     assert not np.array_equal(model_life(a, b, 13, 13, extra_core=1), want)

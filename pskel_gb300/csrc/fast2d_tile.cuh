@@ -156,9 +156,138 @@ struct TileGeom {
   const void* v;
 };
 
+// The tile routine for a tile that touches no ring cell (its whole window
+// lies in the interior): every warp keeps its S rows, and the rows above and
+// below them, in registers for all the steps, with west and east neighbours by
+// shuffles, updates the rows in place top to bottom (the old row above kept
+// aside), and after each step exchanges only its first and last rows with
+// the two neighbouring warps through `xch` (two parities, so one meeting per
+// step suffices, as in the Life kernel). bf16 rows are rounded to bf16 every
+// step, as storing them would. The core rows go from registers to dst.
+template <class TS, int OpK, int S>
+__device__ __forceinline__ void fast2d_run_tile_regs(const TS* sbuf, TS* xch, TS* dst, const TileGeom& g, int gy0,
+                                                     int gx0, const float* wt, const float2* wt2, float2 nz) {
+  constexpr int N = Vec<TS>::N;
+  constexpr int LW = 32 * N;
+  constexpr int LH = kFastWarps * S + 2;
+  constexpr bool kAdvect = (OpK == 3);
+  constexpr auto shp = shape_of<(OpK < 3 ? OpK : 0)>();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x0 = lane * N;
+  const int yb = 1 + warp * S;  // window row of this warp's row 1
+  const TS* wu = static_cast<const TS*>(g.u);
+  const TS* wv = static_cast<const TS*>(g.v);
+  const int gxv = gx0 + x0;
+  float r[S + 2][N];  // window rows yb-1 .. yb+S
+#pragma unroll
+  for (int k = 0; k < S + 2; ++k) ld_vec(sbuf + (yb - 1 + k) * LW + x0, r[k]);
+  int par = 0;
+  for (int s = 1; s <= g.steps; ++s) {
+    // after step s only rows [s, LH - s) are exact; a warp with none of them
+    // computes nothing (it still meets its neighbours below)
+    if (!(yb + S <= s || yb >= LH - s)) {
+      float a[N];  // the row above, as it was before this step
+      float aw, ae, cw, ce;  // west / east neighbours of the row above and of this row
+#pragma unroll
+      for (int c = 0; c < N; ++c) a[c] = r[0][c];
+      aw = __shfl_up_sync(0xFFFFFFFFu, r[0][N - 1], 1);
+      ae = __shfl_down_sync(0xFFFFFFFFu, r[0][0], 1);
+      cw = __shfl_up_sync(0xFFFFFFFFu, r[1][N - 1], 1);
+      ce = __shfl_down_sync(0xFFFFFFFFu, r[1][0], 1);
+#pragma unroll
+      for (int k = 1; k <= S; ++k) {
+        const float bw = __shfl_up_sync(0xFFFFFFFFu, r[k + 1][N - 1], 1);
+        const float be = __shfl_down_sync(0xFFFFFFFFu, r[k + 1][0], 1);
+        const int y = yb - 1 + k;
+        const bool live = y >= s && y < LH - s;
+        float res[N];
+        if (live) {
+          // cell c + dw of the row dh below this one (dh, dw in -1..1)
+          auto at = [&](int dh, int cc) -> float {
+            if (dh < 0) return cc < 0 ? aw : (cc >= N ? ae : a[cc < 0 ? 0 : (cc >= N ? N - 1 : cc)]);
+            if (dh > 0) return cc < 0 ? bw : (cc >= N ? be : r[k + 1][cc < 0 ? 0 : (cc >= N ? N - 1 : cc)]);
+            return cc < 0 ? cw : (cc >= N ? ce : r[k][cc < 0 ? 0 : (cc >= N ? N - 1 : cc)]);
+          };
+          if constexpr (!kAdvect) {
+#pragma unroll
+            for (int c = 0; c < N; c += 2) {
+              float2 acc;
+#pragma unroll
+              for (int n = 0; n < shp.n; ++n) {
+                const int dh = shp.dh[n], dw = shp.dw[n];
+                const float2 t = (dw == 0) ? fmul2_rn(wt2[n], make_float2(at(dh, c), at(dh, c + 1)), nz)
+                                           : make_float2(__fmul_rn(wt[n], at(dh, c + dw)),
+                                                         __fmul_rn(wt[n], at(dh, c + 1 + dw)));
+                acc = (n == 0) ? t : fadd2_rn(acc, t);
+              }
+              res[c] = acc.x;
+              res[c + 1] = acc.y;
+            }
+          } else {
+            float uu[N], vv[N];
+            ld_wind(wu, g.pitch, gy0 + y, gxv, g.W, g.H, uu);
+            ld_wind(wv, g.pitch, gy0 + y, gxv, g.W, g.H, vv);
+#pragma unroll
+            for (int c = 0; c < N; c += 2) {
+              const float2 r2 = advect_pair(make_float2(at(0, c), at(0, c + 1)), make_float2(at(-1, c), at(-1, c + 1)),
+                                            make_float2(at(0, c + 1), at(0, c + 2)),
+                                            make_float2(at(0, c - 1), at(0, c)),
+                                            make_float2(at(1, c), at(1, c + 1)), make_float2(uu[c], uu[c + 1]),
+                                            make_float2(vv[c], vv[c + 1]), g.K, g.dt, g.inv_dx, nz);
+              res[c] = r2.x;
+              res[c + 1] = r2.y;
+            }
+          }
+          if constexpr (sizeof(TS) == 2) {
+#pragma unroll
+            for (int c = 0; c < N; ++c)
+              res[c] = __uint_as_float(static_cast<uint32_t>(__bfloat16_as_ushort(__float2bfloat16_rn(res[c]))) << 16);
+          }
+        }
+        // this row, before the step, is the row above the next one
+#pragma unroll
+        for (int c = 0; c < N; ++c) a[c] = r[k][c];
+        aw = cw;
+        ae = ce;
+        if (live) {
+#pragma unroll
+          for (int c = 0; c < N; ++c) r[k][c] = res[c];
+        }
+        cw = bw;
+        ce = be;
+      }
+    }
+    if (s < g.steps) {
+      // first and last rows to the neighbours; theirs back
+      TS* xb = xch + par * (2 * kFastWarps * LW);
+      st_vec(xb + (2 * warp) * LW + x0, r[1]);
+      st_vec(xb + (2 * warp + 1) * LW + x0, r[S]);
+      neighbours_barrier(warp);
+      if (warp > 0) ld_vec(xb + (2 * (warp - 1) + 1) * LW + x0, r[0]);
+      if (warp < kFastWarps - 1) ld_vec(xb + (2 * (warp + 1)) * LW + x0, r[S + 1]);
+      par ^= 1;
+    }
+  }
+  // core rows [HY, HY + TH), columns [HX, HX + TW) to dst: a lane's N cells
+  // lie all inside or all outside (HX and TW are multiples of N)
+  if (x0 >= g.HX && x0 < g.HX + g.TW) {
+#pragma unroll
+    for (int k = 1; k <= S; ++k) {
+      const int y = yb - 1 + k;
+      if (y >= g.HY && y < g.HY + g.TH) st_vec(dst + static_cast<int64_t>(gy0 + y) * g.pitch + gxv, r[k]);
+    }
+  }
+}
+
 // Runs g.steps steps on a staged tile (source tile in sbuf, the partner
 // buffer pbuf holding the destination's ring when the tile touches it), then
 // writes the core's interior cells to dst. All threads of the block call it.
+// An fp32 tile clear of the ring takes the register-resident routine above
+// (pbuf, unused then, holds its row exchange). Measured on GB300 against this
+// shared-memory routine (GCells/s): advection 4096^2 T=5 453 -> 476, batched
+// Jacobi fp32 813 -> 846, Jacobi 1024^2 fp32 708 -> 703; bf16 (rounded in
+// registers every step) Jacobi 653 -> 626, batch 782 -> 783, so bf16 keeps
+// the shared-memory routine.
 template <class TS, int OpK, int S>
 __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, const TileGeom& g, int gy0, int gx0,
                                                 bool ring_tile, const float* wt, float2 nz) {
@@ -177,6 +306,12 @@ __device__ __forceinline__ void fast2d_run_tile(TS* sbuf, TS* pbuf, TS* dst, con
   float2 wt2[shp.n > 0 ? shp.n : 1];
 #pragma unroll
   for (int n = 0; n < shp.n; ++n) wt2[n] = make_float2(wt[n], wt[n]);
+  if constexpr (sizeof(TS) == 4) {
+    if (!ring_tile) {
+      fast2d_run_tile_regs<TS, OpK, S>(sbuf, pbuf, dst, g, gy0, gx0, wt, wt2, nz);
+      return;
+    }
+  }
   for (int s = 1; s <= g.steps; ++s) {
     const TS* in = ((s & 1) ? sbuf : pbuf);
     TS* out = ((s & 1) ? pbuf : sbuf);

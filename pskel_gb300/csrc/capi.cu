@@ -727,7 +727,7 @@ static pskel_status stream3d_cross7(const pskel_stencil& st, Stencil3DParams& p,
     p.partials = p2.partials = part;
   }
   // the grid as 32-bit words: a 16-byte vector is 4 words for either dtype;
-  // boxes of 136 words x (16 rows + the halo rows of the kernel) x 1 plane
+  // boxes of 136 words x (16 w rows + the halo rows of the kernel) x 1 plane
   CUtensorMap maps1[2], maps2[2];
   const uint64_t dims[3] = {static_cast<uint64_t>(D) * esz / 4, static_cast<uint64_t>(W), static_cast<uint64_t>(H)};
   const uint64_t strides[2] = {static_cast<uint64_t>(D) * esz, static_cast<uint64_t>(D) * esz * W};

@@ -13,11 +13,15 @@
 // plus a copy of the row above and below. West/east neighbour words come
 // from the adjacent lanes by warp shuffles, rows above/below from the
 // lane's own registers; after each step the warps of a block exchange their
-// first and last rows through shared memory. A step costs per 32-cell word
-// 2 shuffles, 2 funnel shifts and 10 LOP3s (row sums shared by the three rows
-// that use them, bit-sliced full adders). Tiles are staged straight from L2
-// into registers with 32-bit ld.global.cg (one load per word per pass:
-// there is no shared-memory copy of the tile to stage into).
+// first and last rows through shared memory, each warp meeting only its two
+// neighbours (pairwise named barriers). A step costs per 32-cell word 2
+// shuffles, 2 funnel shifts and 10 LOP3s (row sums shared by the three rows
+// that use them, bit-sliced full adders). Work items (pass, tile) come from an
+// atomic counter; a producer warp takes the next item, waits (bounded) until
+// the tiles of the previous pass its window reads are done, and loads the
+// window from L2 into shared memory by 2D TMA (boxes of at most 256 rows)
+// while the consumer warps step the current tile; they then copy it into
+// their registers.
 //
 // Ring cells (outside r <= h < H-r, r <= w < W-r) are never updated, the
 // semantics of Stencil2D::runOpenMP (PSkelStencil.hpp:2197-2257): in the

@@ -14,7 +14,8 @@
 //
 // Each tile is processed by the register-windowed tile routine of the
 // single-grid kernel (fast2d_tile.cuh): TMA-staged source tile, destination
-// tile for ring tiles, T steps in shared memory, interior cells written back.
+// tile for ring tiles, T steps in shared memory (in registers for fp32 tiles
+// clear of the ring), interior cells written back.
 #include <cudaTypedefs.h>
 
 #include <algorithm>

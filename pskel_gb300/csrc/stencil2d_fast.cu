@@ -14,8 +14,10 @@
 // the core never reaches in T <= halo steps; step s computes the full width
 // and only the rows [s, LH - s) that are still exact.
 //
-// Arithmetic is the oracle's: products and sums in mask order with
-// __fmul_rn/__fadd_rn (no contraction), bf16 results rounded every step.
+// fp32 tiles clear of the ring keep their rows in registers between steps
+// instead (fast2d_tile.cuh). Arithmetic is the oracle's: products and sums in
+// mask order, unfused (two neighbouring cells per instruction with the paired
+// fp32 forms of common.cuh), bf16 results rounded every step.
 #include <atomic>
 
 #include "fast2d_tile.cuh"

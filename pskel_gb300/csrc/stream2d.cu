@@ -5,8 +5,9 @@
 // ring <= h < H-ring and ring <= w < W-ring are written, so each buffer keeps
 // its own ring, as in Stencil2D::runOpenMP (PSkelStencil.hpp:2197-2257).
 //
-// Arithmetic is the oracle's: products and sums in mask order with
-// __fmul_rn/__fadd_rn (no contraction), bf16 results rounded every step.
+// Arithmetic is the oracle's: products and sums in mask order, unfused
+// (two neighbouring cells per instruction with the paired fp32 forms of
+// common.cuh), bf16 results rounded every step.
 #include "fast2d_tile.cuh"
 
 namespace pskel {

@@ -255,7 +255,7 @@ static pskel_status iterate_life(const pskel_stencil& st, void* in, void* out, i
   }
   const int64_t tiles = life_bits_tiles(static_cast<int>(W), static_cast<int>(H), g.TH);
   // every pass in one persistent launch: no more CTAs than can be resident
-  const int64_t resident = static_cast<int64_t>(life_bits_persistent_ctas_per_sm()) * c->sms;
+  const int64_t resident = static_cast<int64_t>(life_bits_persistent_ctas_per_sm(g.T)) * c->sms;
   int ctas = (sched && sched->ctas > 0) ? sched->ctas : static_cast<int>(resident);
   ctas = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(ctas, resident), tiles)));
   const size_t plane = static_cast<size_t>(life_bits_words(static_cast<int>(W))) * static_cast<size_t>(H);
@@ -1075,7 +1075,7 @@ static pskel_status run_life_host_wavefront(const uint8_t* in_host, uint8_t* out
   uint32_t* Y = X + plane;
   const int Wi = static_cast<int>(W), Hi = static_cast<int>(H);
   const int64_t pitch = static_cast<int64_t>(pitch_bytes);
-  const int64_t resident = static_cast<int64_t>(life_bits_persistent_ctas_per_sm()) * c->sms;
+  const int64_t resident = static_cast<int64_t>(life_bits_persistent_ctas_per_sm(T)) * c->sms;
   cudaStream_t s = c->stream, s_in = c->copy_in, s_out = c->copy_out;
   StreamDrain drain{s_in, s_out};
   const int CT = (tiles_y + kLifeChunks - 1) / kLifeChunks;  // tile rows per chunk

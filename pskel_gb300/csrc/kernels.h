@@ -25,19 +25,24 @@ std::vector<int> plan_passes(int64_t iters, int T);
 // life_bits_words(W) words), run the passes between the planes, unpack the
 // final plane's interior into the result buffer. A tile is one warp of words
 // wide (kLifeCoreWords core words, one halo word each side) and holds a
-// window of kLifeWindowRows rows in registers (kLifeWarps consumer warps x
-// kLifeRows rows, plus one row above and below); after T <= kLifeBitsMaxT
-// steps its core of TH <= life_bits_max_tile_h(T) = kLifeWindowRows - 2T rows
-// is exact.
+// window of life_bits_window_rows(T) rows in registers (kLifeWarps consumer
+// warps x life_bits_rows(T) rows, plus one row above and below); after
+// T <= kLifeBitsMaxT steps its core of TH <= life_bits_max_tile_h(T) =
+// life_bits_window_rows(T) - 2T rows is exact. Passes of kLifeTallT steps or
+// more use the taller window (its halo rows are a smaller share), shorter
+// passes the shorter one (less to load per step).
 constexpr int kLifeBitsMaxT = 31;
-constexpr int kLifeRows = 24;
+constexpr int kLifeRowsTall = 24;
+constexpr int kLifeRowsShort = 16;
+constexpr int kLifeTallT = 15;
 constexpr int kLifeWarps = 15;
 constexpr int kLifeCoreWords = 30;
-constexpr int kLifeWindowRows = kLifeWarps * kLifeRows + 2;
+constexpr int life_bits_rows(int T) { return T >= kLifeTallT ? kLifeRowsTall : kLifeRowsShort; }
+constexpr int life_bits_window_rows(int T) { return kLifeWarps * life_bits_rows(T) + 2; }
 int life_bits_words(int W);
 int life_bits_tiles_x(int W);
 int life_bits_max_tile_h(int T);
-size_t life_bits_smem_bytes();
+size_t life_bits_smem_bytes(int T);
 int life_bits_tiles(int W, int H, int TH);
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
                            unsigned* err, int sms, cudaStream_t s);
@@ -47,7 +52,7 @@ cudaError_t life_bits_unpack(const uint32_t* plane, uint8_t* dst, int64_t pitch,
 // 1 + 2 * (q + (i < r)) steps and reads X (even i) or Y (odd i). Tiles wait
 // (bounded) for their neighbours' previous pass; `sync` holds the item
 // counter and per-tile completion counts (life_bits_sync_bytes, cleared here).
-// ctas must not exceed the resident CTAs (life_bits_persistent_ctas_per_sm).
+// ctas must not exceed the resident CTAs (life_bits_persistent_ctas_per_sm(T)).
 size_t life_bits_sync_bytes(int W, int H, int TH);
 // A launch's share of the passes of a run: passes pass0 .. pass0+np-1, each
 // over every tile, or (windowed) pass pass0+j over the tile rows
@@ -73,7 +78,7 @@ cudaError_t life_bits_pack_rows(const uint8_t* src, int64_t pitch, int W, int H,
                                 int row0, int row1, unsigned* err, int sms, cudaStream_t s);
 cudaError_t life_bits_unpack_rows(const uint32_t* plane, uint8_t* dst, int64_t pitch, int W, int H, int ring,
                                   int row0, int row1, int sms, cudaStream_t s);
-int life_bits_persistent_ctas_per_sm();
+int life_bits_persistent_ctas_per_sm(int T);
 cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int ring, int npasses, int q, int r,
                                      int T, int TH, int ctas, void* sync, unsigned* err, cudaStream_t s);
 

@@ -9,8 +9,9 @@
 // A pass advances a tile by up to 31 steps with the tile held in registers:
 // one warp spans 32 words (1024 cells) of a tile row, lane l holding word
 // 30*tx - 1 + l (lanes 1..30 are the tile's core, lanes 0 and 31 its one-word
-// halo), and each lane holds a column of kLifeRows words of its warp's rows
-// plus a copy of the row above and below. West/east neighbour words come
+// halo), and each lane holds a column of R words of its warp's rows (R = 24
+// for passes of 15 steps or more, 16 for shorter ones) plus a copy of the
+// row above and below. West/east neighbour words come
 // from the adjacent lanes by warp shuffles, rows above/below from the
 // lane's own registers; after each step the warps of a block exchange their
 // first and last rows through shared memory, each warp meeting only its two
@@ -83,9 +84,9 @@ constexpr uint32_t kNotAAndBxC = 0x06;  // ~a & (b ^ c)
 constexpr uint32_t kAAndBorC = 0xE0;  // a & (b | c)
 constexpr uint32_t kSelect = 0xCA;    // a ? b : c, bitwise
 
-// Register-resident tile geometry (kernels.h: kLifeRows, kLifeWarps,
-// kLifeCoreWords): consumer warp w of a block holds rows w*kLifeRows ..
-// w*kLifeRows + kLifeRows + 1 of the tile's window of kLifeWindowRows rows.
+// Register-resident tile geometry (kernels.h: life_bits_rows, kLifeWarps,
+// kLifeCoreWords): with R rows per lane, consumer warp w of a block holds
+// rows w*R .. w*R + R + 1 of the tile's window of kLifeWarps*R + 2 rows.
 static_assert(kLifeCoreWords == 30, "a tile is one warp of words with one halo word each side");
 
 // Row sums of one row for the bit-sliced neighbour count: with we / ea the
@@ -103,7 +104,7 @@ __device__ __forceinline__ void row_sums(uint32_t c, uint32_t& t0, uint32_t& t1,
   p1 = we & ea;
 }
 
-// One step of a warp's rows 1..kLifeRows from rows 0..kLifeRows+1, in place.
+// One step of a warp's rows 1..R from rows 0..R+1, in place.
 // The neighbour count of a cell is (row above: t) + (its row: p) + (row
 // below: t); the three 2-bit numbers are added with full adders: s0 = low
 // bit, k0 = its carry, x1/y1 = sum/carry of the twos. With k0 folded in,
@@ -502,19 +503,28 @@ __global__ void __launch_bounds__(LifeGeo<R, NW>::kThreads, kMinBlocks)
 
 namespace {
 
-// The kernel as launched: kLifeRows rows per lane, kLifeWarps consumer warps,
-// one block per SM. Measured on GB300 (8192^2, 1000 generations): 24 rows x
-// 15 warps (128 registers: the register file exactly; a 362-row window in two
-// TMA boxes) 27.7 T updates/s at T = 17; 16 rows x 15 warps (242 rows, one
-// box) 27.4 T at T = 13, 27.3 T at T = 15; 8 rows x 15 warps
-// at two blocks per SM 21.5 T (T = 7, the best T for it; its windows are half
-// as tall, so the halo rows and the per-step exchange cost twice as much per
-// row); 16 rows x 7 warps at two blocks per SM 22.5 T. The row shifts as
-// integer multiply-adds on the idle FMA pipe (by 2 and 2^31 from a kernel
-// argument) instead of funnel shifts on the ALU pipe: 23.3 T.
-using LifeKernelGeo = LifeGeo<kLifeRows, kLifeWarps>;
+// The kernels as launched: life_bits_rows(T) rows per lane, kLifeWarps
+// consumer warps, one block per SM. Measured on GB300 (8192^2, 1000
+// generations): 24 rows x 15 warps (128 registers: the register file
+// exactly; a 362-row window in two TMA boxes) 27.7 T updates/s at T = 17;
+// 16 rows x 15 warps (242 rows, one box) 27.4 T at T = 13, 27.3 T at T = 15,
+// and at one step per pass 9.1 T against 7.6 T for the 24-row window; 8 rows
+// x 15 warps at two blocks per SM 21.5 T (T = 7, the best T for it; its
+// windows are half as tall, so the halo rows and the per-step exchange cost
+// twice as much per row); 16 rows x 7 warps at two blocks per SM 22.5 T. The
+// row shifts as integer multiply-adds on the idle FMA pipe (by 2 and 2^31
+// from a kernel argument) instead of funnel shifts on the ALU pipe: 23.3 T.
 constexpr int kLifeMinBlocks = 1;
-const auto life_kernel = life_bits_persistent_kernel<kLifeRows, kLifeWarps, kLifeMinBlocks>;
+static_assert(life_bits_rows(kLifeBitsMaxT) == kLifeRowsTall && life_bits_rows(1) == kLifeRowsShort, "geometries");
+
+template <int R>
+struct LifeKernel {
+  using G = LifeGeo<R, kLifeWarps>;
+  static constexpr auto fn = life_bits_persistent_kernel<R, kLifeWarps, kLifeMinBlocks>;
+  static cudaError_t allow_smem() {
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(G::kSmemBytes));
+  }
+};
 
 }  // namespace
 
@@ -522,11 +532,14 @@ int life_bits_words(int W) { return ((W + 31) / 32 + 3) & ~3; }
 
 int life_bits_tiles_x(int W) { return (life_bits_words(W) + kLifeCoreWords - 1) / kLifeCoreWords; }
 
-int life_bits_max_tile_h(int T) { return LifeKernelGeo::kWindowRows - 2 * T; }
+int life_bits_max_tile_h(int T) { return life_bits_window_rows(T) - 2 * T; }
 
 int life_bits_tiles(int W, int H, int TH) { return life_bits_tiles_x(W) * ((H + TH - 1) / TH); }
 
-size_t life_bits_smem_bytes() { return LifeKernelGeo::kSmemBytes; }
+size_t life_bits_smem_bytes(int T) {
+  return life_bits_rows(T) == kLifeRowsTall ? LifeKernel<kLifeRowsTall>::G::kSmemBytes
+                                            : LifeKernel<kLifeRowsShort>::G::kSmemBytes;
+}
 
 
 cudaError_t life_bits_pack(const uint8_t* src, int64_t pitch, int W, int H, uint32_t* plane, int ring, bool ring_only,
@@ -562,13 +575,20 @@ size_t life_bits_sync_bytes(int W, int H, int TH) {
   return 16 + sizeof(unsigned) * static_cast<size_t>(life_bits_tiles(W, H, TH));
 }
 
-int life_bits_persistent_ctas_per_sm() {
+namespace {
+template <int R>
+int life_ctas_per_sm() {
+  using K = LifeKernel<R>;
   int n = 0;
-  const size_t smem = LifeKernelGeo::kSmemBytes;
-  cudaFuncSetAttribute(life_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, life_kernel, LifeKernelGeo::kThreads, smem) != cudaSuccess)
+  K::allow_smem();
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, K::fn, K::G::kThreads, K::G::kSmemBytes) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
+}
+}  // namespace
+
+int life_bits_persistent_ctas_per_sm(int T) {
+  return life_bits_rows(T) == kLifeRowsTall ? life_ctas_per_sm<kLifeRowsTall>() : life_ctas_per_sm<kLifeRowsShort>();
 }
 
 cudaError_t life_bits_run_persistent(uint32_t* X, uint32_t* Y, int W, int H, int ring, int npasses, int q, int r,
@@ -606,13 +626,18 @@ cudaError_t life_bits_run_window(uint32_t* X, uint32_t* Y, int W, int H, int rin
   CUtensorMap mx, my;
   const uint64_t dims[2] = {static_cast<uint64_t>(PW), static_cast<uint64_t>(H)};
   const uint64_t strides[1] = {static_cast<uint64_t>(PW) * 4};
-  const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(LifeKernelGeo::kBoxRows)};
-  cudaError_t e = encode_tmap(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, X, dims, strides, box);
-  if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
-  if (e != cudaSuccess) return e;
-  life_kernel<<<ctas, LifeKernelGeo::kThreads, LifeKernelGeo::kSmemBytes, s>>>(
-      mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y, next, done, err, win, spin_limit);
-  return cudaGetLastError();
+  auto launch = [&](auto kernel) -> cudaError_t {
+    using K = decltype(kernel);
+    const uint32_t box[2] = {static_cast<uint32_t>(kLifeBoxWords), static_cast<uint32_t>(K::G::kBoxRows)};
+    cudaError_t e = encode_tmap(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, X, dims, strides, box);
+    if (e == cudaSuccess) e = encode_tmap(&my, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, Y, dims, strides, box);
+    if (e == cudaSuccess) e = K::allow_smem();
+    if (e != cudaSuccess) return e;
+    K::fn<<<ctas, K::G::kThreads, K::G::kSmemBytes, s>>>(mx, my, X, Y, PW, W, H, ring, q, r, T, TH, tiles_x, tiles_y,
+                                                         next, done, err, win, spin_limit);
+    return cudaGetLastError();
+  };
+  return life_bits_rows(T) == kLifeRowsTall ? launch(LifeKernel<kLifeRowsTall>{}) : launch(LifeKernel<kLifeRowsShort>{});
 }
 
 }  // namespace pskel

@@ -107,7 +107,7 @@ pskel_status pskel_selftest_bounded_wait(int32_t which, uint32_t polls, void* st
   win.pass0 = 1;
   win.np = 1;
   const int ctas = static_cast<int>(std::min<int64_t>(life_bits_tiles(W, H, TH),
-                                                      static_cast<int64_t>(life_bits_persistent_ctas_per_sm()) * c->sms));
+                                                      static_cast<int64_t>(life_bits_persistent_ctas_per_sm(T)) * c->sms));
   e = life_bits_run_window(X, X + plane, W, H, 1, win, 1, 0, T, TH, ctas, c->life_sync.ptr, c->err, s, true, polls);
   return e == cudaSuccess ? PSKEL_OK : cuda_fail(e, "selftest launch");
 }

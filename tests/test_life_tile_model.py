@@ -25,9 +25,10 @@ import pytest
 from pskel_gb300 import synth as S
 
 CORE = 30  # core words per tile (kernels.h)
-# (consumer warps per block, rows per lane): the kernel's geometry (kernels.h)
-# first; a window half as tall checks the same scheme with more tiles
-VARIANTS = [(15, 24), (15, 8)]
+# (consumer warps per block, rows per lane): the kernel's two geometries
+# (kernels.h: 24 rows for passes of 15 steps or more, 16 for shorter ones)
+# first; a window a third as tall checks the same scheme with more tiles
+VARIANTS = [(15, 24), (15, 16), (15, 8)]
 
 
 def words(W):

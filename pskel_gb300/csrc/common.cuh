@@ -174,6 +174,30 @@ struct Vec16 {
   __device__ __forceinline__ void fill(uint32_t h) { r[0] = r[1] = r[2] = r[3] = h; }
 };
 
+// The one edge cell a lane needs from a staged row laid out as a 16-byte
+// west halo vector, 32 core vectors (one per lane) and a 16-byte east halo
+// vector: lane 0 the cell before the first core cell (the last cell of the
+// west vector, in bytes 12..15), lane 31 the cell after the last one (the
+// first cell of the east vector, at byte 16 + 32*16). Every lane issues the
+// same one 4-byte shared load (lanes 1..30 take lane 0's word, a broadcast,
+// and ignore it) and, for bf16, one byte permute that widens its half of the
+// word -- instead of two predicated loads and widenings per row.
+template <class TS>
+struct EdgeCell {
+  int off;       // byte offset of the lane's word within the row
+  uint32_t sel;  // __byte_perm selector: the cell's 16 bits to the top, zeros below
+  __device__ __forceinline__ explicit EdgeCell(int lane)
+      : off(lane == 31 ? 16 + 32 * 16 : 12), sel(lane == 31 ? 0x1044u : 0x3244u) {}
+  __device__ __forceinline__ float get(const uint8_t* row) const {
+    const uint32_t w = *reinterpret_cast<const uint32_t*>(row + off);
+    if constexpr (sizeof(TS) == 4) {
+      return __uint_as_float(w);
+    } else {
+      return __uint_as_float(__byte_perm(w, 0u, sel));
+    }
+  }
+};
+
 // Paired fp32 arithmetic (Blackwell's add/sub/fma.f32x2): two lanes per
 // instruction, each rounded to nearest like the scalar .rn forms, so every lane
 // matches the reference's unfused scalar arithmetic bit for bit -- provided no

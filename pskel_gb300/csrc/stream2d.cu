@@ -131,7 +131,9 @@ __global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __gri
   int s_next = 0;
   uint32_t ph_next = 0;
   // the row `r` (0..7, or 8+ for the next box) of the group's staged phi rows
-  auto ld_row = [&](int slot_a, int slot_b, int r, Vt& v, float& l, float& e) {
+  // and the row's edge cell for lane 0 (west) / lane 31 (east)
+  const EdgeCell<TS> edge(lane);
+  auto ld_row = [&](int slot_a, int slot_b, int r, Vt& v, float& h) {
     const int sl = (r < kR2Rows) ? slot_a : slot_b;
     const int rr = (r < kR2Rows) ? r : r - kR2Rows;
     const uint8_t* row = smem_raw + sl * kStride + rr * (16 + 512 + 16);
@@ -140,8 +142,7 @@ __global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __gri
     v.r[1] = x.y;
     v.r[2] = x.z;
     v.r[3] = x.w;
-    l = (lane == 0) ? Storage<TS>::load(*reinterpret_cast<const TS*>(row + 16 - ES)) : 0.0f;
-    e = (lane == 31) ? Storage<TS>::load(*reinterpret_cast<const TS*>(row + 16 + 512)) : 0.0f;
+    h = edge.get(row);
   };
   bool alive = true;
   for (int64_t it = blockIdx.x; it < items && alive; it += gridDim.x) {
@@ -169,9 +170,9 @@ __global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __gri
       const int rbase = hs + kR2Rows * k + warp * kR2RW;
       // staged rows rbase-1 .. rbase+kR2RW, with their west and east neighbours
       Vt rows[kR2RW + 2];
-      float rw[kR2RW + 2], re[kR2RW + 2];
+      float rh[kR2RW + 2];
 #pragma unroll
-      for (int q = 0; q < kR2RW + 2; ++q) ld_row(s_a, s_b, warp * kR2RW + q, rows[q], rw[q], re[q]);
+      for (int q = 0; q < kR2RW + 2; ++q) ld_row(s_a, s_b, warp * kR2RW + q, rows[q], rh[q]);
       Vt uu[kR2RW], vv[kR2RW];
       if constexpr (kAdvect) {
 #pragma unroll
@@ -191,8 +192,8 @@ __global__ void __launch_bounds__(kR2Threads, 4) stream2d_tma_kernel(const __gri
       for (int q = 0; q < kR2RW + 2; ++q) {
         wq[q] = __shfl_up_sync(0xFFFFFFFFu, rows[q].at(V - 1), 1);
         eq[q] = __shfl_down_sync(0xFFFFFFFFu, rows[q].at(0), 1);
-        if (lane == 0) wq[q] = rw[q];
-        if (lane == 31) eq[q] = re[q];
+        if (lane == 0) wq[q] = rh[q];
+        if (lane == 31) eq[q] = rh[q];
       }
       auto val = [&](int q, int kk) -> float {
         return (kk < 0) ? wq[q] : (kk >= V ? eq[q] : rows[q].at(kk));

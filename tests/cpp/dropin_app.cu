@@ -4,6 +4,7 @@
 //   dropin_app SCENARIO W H D ITERS IN OUTINIT RESULT [RESIDUALS]
 //
 // Grids are raw files in the reference's layouts; D is 1 for 2D scenarios.
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -140,6 +141,43 @@ int main(int argc, char** argv) {
   const size_t W = std::strtoull(argv[2], 0, 10), H = std::strtoull(argv[3], 0, 10), D = std::strtoull(argv[4], 0, 10);
   const size_t it = std::strtoull(argv[5], 0, 10);
   const char *fin = argv[6], *fout = argv[7], *fres = argv[8];
+
+  if (sc == "map1d_time" || sc == "stencil1d_time") {
+    // Throughput through the public API: W cells, runIterativeGPU(it / 100)
+    // and runIterativeGPU(it) timed on the host (each call copies the array in
+    // and the result out); the difference of the two, divided by the
+    // difference of the iteration counts, is the time of one iteration on the
+    // device. Prints one JSON line: microseconds and GB/s per iteration (8
+    // bytes per cell: one read, one write).
+    Array<float> in(W), out(W);
+    for (size_t i = 0; i < W; ++i) {
+      in.hostArray[i] = static_cast<float>(i % 1000) * 0.001f;
+      out.hostArray[i] = 0.5f;
+    }
+    Mask<float> mask(5, 0.5f);
+    const int off[5] = {-2, -1, 0, 1, 3};
+    const float wt[5] = {0.125f, 0.25f, 0.3f, 0.2f, 0.125f};
+    for (int n = 0; n < 5; ++n) mask.set(n, off[n], wt[n]);
+    Map<Array<float>, Affine> m(in, out, Affine{0.75f, 0.125f});
+    Stencil<Array<float>, Mask<float>, Smooth1D> st(in, out, mask, Smooth1D{0});
+    const bool is_map = sc == "map1d_time";
+    auto run = [&](size_t n) -> double {
+      const auto t0 = std::chrono::steady_clock::now();
+      if (is_map)
+        m.runIterativeGPU(n, 0);
+      else
+        st.runIterativeGPU(n, 0, 0);
+      return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    };
+    const size_t it1 = it / 100 > 0 ? it / 100 : 1;
+    run(2);  // warm-up
+    const double t1 = run(it1), t2 = run(it);
+    const double us = (t2 - t1) / static_cast<double>(it - it1) * 1e6;
+    std::printf("{\"scenario\": \"%s\", \"cells\": %zu, \"iterations\": [%zu, %zu], \"seconds\": [%.6f, %.6f], "
+                "\"us_per_iteration\": %.3f, \"GBps\": %.1f}\n",
+                is_map ? "map1d" : "stencil1d", W, it1, it, t1, t2, us, 8.0 * static_cast<double>(W) / us * 1e-3);
+    return it > it1 ? 0 : 3;
+  }
 
   if (sc.rfind("jacobi", 0) == 0) {
     Array2D<float> in(W, H), out(W, H);

@@ -13,6 +13,7 @@ fused multiply-add by default, which the oracle does not do.
 """
 from __future__ import annotations
 
+import json
 import subprocess
 import tempfile
 from pathlib import Path
@@ -252,3 +253,17 @@ def test_dropin_args_field_out_of_core(app, iters):
     got, _ = run_app(app, "coef_tiling", a, b, iters, env=env, stdout=out)
     assert "out of core" in out[0]
     assert np.array_equal(got.view(np.uint32), coef_run(a, b, iters).view(np.uint32))
+
+
+@pytest.mark.parametrize("scenario", ["map1d_time", "stencil1d_time"])
+def test_dropin_functor_throughput(app, scenario):
+    """The grid-stride user-functor kernels (the Map skeleton and the 1D
+    stencil) measured through the public API on 2^27 cells: one iteration's
+    device time is the difference of two runs of different lengths divided by
+    the difference of their iteration counts. A floor only (the kernels read
+    and write each cell once per iteration, one cell per thread)."""
+    r = subprocess.run([str(app), scenario, str(1 << 27), "1", "1", "1000", "-", "-", "-"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["iterations"] == [10, 1000] and line["GBps"] > 500, line

@@ -40,6 +40,12 @@ inline void pskelAssert(pskel_status code, const char* file, int line) {
   }
 }
 
+#ifdef __CUDACC__
+// An L2 prefetch hint for an address that a grid-stride kernel will read a
+// few iterations later (generic address; a hint only: no value changes).
+__device__ __forceinline__ void pskel_prefetch_l2(const void* p) { asm volatile("prefetch.L2 [%0];" ::"l"(p)); }
+#endif
+
 }  // namespace PSkel
 
 #define gpuErrchk(ans) \

@@ -32,12 +32,22 @@ namespace detail {
 
 #ifdef __CUDACC__
 // One thread per element, grid-stride; (h, w, d) from the flat index with d
-// fastest, the reference's layout (PSkelArray.hpp:349-352, 658-677).
+// fastest, the reference's layout (PSkelArray.hpp:349-352, 658-677). Where
+// the input array is dense (flat index i at deviceArray[i]), each thread
+// hints the input element of its iteration two ahead into L2: with one cell
+// per thread and the user functor's store between loads, a thread otherwise
+// has a single load in flight.
 template <int Dim, class Arrays, class Args>
 __global__ void map_kernel(Arrays in, Arrays out, Args args, size_t W, size_t H, size_t D) {
   const size_t n = W * H * D;
-  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  const bool dense = in.pskel_org_h == 0 && in.pskel_org_w == 0 && in.pskel_org_d == 0 &&
+                     (Dim == 1 || in.pskel_pitch_w == static_cast<long>(W)) &&
+                     (Dim < 3 || in.pskel_pitch_d == static_cast<long>(D));
+  size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+  if (dense && i + stride < n) pskel_prefetch_l2(in.deviceArray + i + stride);
+  for (; i < n; i += stride) {
+    if (dense && i + 2 * stride < n) pskel_prefetch_l2(in.deviceArray + i + 2 * stride);
     if constexpr (Dim == 1) {
       mapKernel(in, out, args, i);
     } else if constexpr (Dim == 2) {

@@ -178,6 +178,36 @@ int main(int argc, char** argv) {
                 is_map ? "map1d" : "stencil1d", W, it1, it, t1, t2, us, 8.0 * static_cast<double>(W) / us * 1e-3);
     return it > it1 ? 0 : 3;
   }
+  if (sc == "coef_time") {
+    // The Args2D functor (a coefficient per cell read from mapped pinned host
+    // memory, as the reference keeps Args fields) on W x H cells, timed like
+    // the scenarios above; bytes per cell: 4 (in) + 4 (out) from HBM and 4
+    // (the coefficient) over the host link.
+    Array2D<float> in(W, H), out(W, H);
+    for (size_t i = 0; i < W * H; ++i) {
+      in.hostArray[i] = static_cast<float>(i % 1000) * 0.001f;
+      out.hostArray[i] = 0.5f;
+    }
+    CoefArgs args{Args2D<float>(static_cast<int>(W), static_cast<int>(H))};
+    for (size_t h = 0; h < H; ++h)
+      for (size_t w = 0; w < W; ++w) args.coef(static_cast<int>(w), static_cast<int>(h)) = 0.05f;
+    Mask2D<float> mask = jacobi_mask();
+    Stencil2D<Array2D<float>, Mask2D<float>, CoefArgs> st(in, out, mask, args);
+    auto run = [&](size_t n) -> double {
+      const auto t0 = std::chrono::steady_clock::now();
+      st.runIterativeGPU(n, 0, 0);
+      return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    };
+    const size_t it1 = it / 10 > 0 ? it / 10 : 1;
+    run(2);
+    const double t1 = run(it1), t2 = run(it);
+    const double us = (t2 - t1) / static_cast<double>(it - it1) * 1e6;
+    const double cells = static_cast<double>(W) * static_cast<double>(H);
+    std::printf("{\"scenario\": \"coef2d\", \"cells\": %.0f, \"iterations\": [%zu, %zu], \"seconds\": [%.6f, %.6f], "
+                "\"us_per_iteration\": %.3f, \"GCells_per_s\": %.1f, \"host_link_GBps\": %.1f}\n",
+                cells, it1, it, t1, t2, us, cells / us * 1e-3, 4.0 * cells / us * 1e-3);
+    return it > it1 ? 0 : 3;
+  }
 
   if (sc.rfind("jacobi", 0) == 0) {
     Array2D<float> in(W, H), out(W, H);

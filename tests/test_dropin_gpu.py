@@ -267,3 +267,14 @@ def test_dropin_functor_throughput(app, scenario):
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["iterations"] == [10, 1000] and line["GBps"] > 500, line
+
+
+def test_dropin_args_field_throughput(app):
+    """The Args2D functor (a per-cell coefficient read from mapped pinned host
+    memory) measured through the public API on 8192 x 4096 cells: it is bound
+    by the host link (4 bytes per cell and iteration over it). A floor only."""
+    r = subprocess.run([str(app), "coef_time", "8192", "4096", "1", "110", "-", "-", "-"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["iterations"] == [11, 110] and line["host_link_GBps"] > 20, line
